@@ -1,0 +1,88 @@
+"""ctypes binding of libattgb300.so (the C ABI declared in include/att_gb300.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, every op raises.
+"""
+import ctypes
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libattgb300.so")
+
+# enum att_dtype
+F32, F16, BF16, F8E4M3, I32, NONE = 0, 1, 2, 3, 4, -1
+# enum att_status
+OK = 0
+
+_c_i64 = ctypes.c_int64
+_c_int = ctypes.c_int
+_c_vp = ctypes.c_void_p
+_c_sz = ctypes.c_size_t
+
+_SIGNATURES = {
+    "att_status_string": (ctypes.c_char_p, [_c_int]),
+    "att_last_error": (ctypes.c_char_p, []),
+    "att_version": (_c_int, []),
+    "att_block_workspace_bytes": (_c_sz, [_c_i64, _c_i64, _c_i64, _c_int]),
+    "att_block_plan": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int, _c_int,
+                                _c_int, _c_vp, _c_sz, ctypes.POINTER(_c_i64),
+                                ctypes.POINTER(_c_i64), _c_vp]),
+    "att_block_fill": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int, _c_int,
+                                _c_int, _c_vp, _c_int, _c_vp, _c_sz, _c_vp, _c_vp, _c_vp, _c_int,
+                                _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "att_spmm": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_i64, _c_vp, _c_int,
+                          _c_vp, _c_i64, _c_i64, _c_i64, _c_vp, _c_i64, _c_i64, _c_int, _c_int,
+                          _c_vp, _c_vp]),
+}
+
+_lib = None
+
+
+class AttError(RuntimeError):
+    """A C-ABI call returned a non-zero att_status."""
+
+    def __init__(self, fn, status, msg):
+        super().__init__("%s failed (status %d: %s): %s" % (fn, status, _status_name(status), msg))
+        self.status = status
+
+
+def _status_name(status):
+    try:
+        return lib().att_status_string(status).decode()
+    except Exception:  # pragma: no cover - library unavailable
+        return "?"
+
+
+def declared_symbols():
+    return sorted(_SIGNATURES)
+
+
+def load(path=None):
+    """Load the shared library (raises OSError if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise OSError("libattgb300.so not built (expected at %s); run "
+                      "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    handle = ctypes.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = handle
+    return _lib
+
+
+def lib():
+    return load()
+
+
+def call(name, *args):
+    """Call a C-ABI function; raise AttError on a non-zero status."""
+    fn = getattr(lib(), name)
+    status = fn(*args)
+    if status != OK:
+        raise AttError(name, status, lib().att_last_error().decode())
+    return status

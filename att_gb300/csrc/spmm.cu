@@ -1,0 +1,596 @@
+// spmm.cu -- blocked SpMM Y = A_blocks * X on the row-window block format.
+//
+// Replaces the reference's GCN SpMM kernels (gcn/SpMM/src/spmmKernel.cu:158-265
+// fp16, :959-1075 tf32, :2066-2330 the "_acc" variants) behind
+// SpMM_sr_bcrs.forward_{fp16,tf32}_gnn[_acc] (gcn/SpMM/src/benchmark.cpp:35-335).
+//
+// Design (sm_103a):
+//  * One warp owns one work item = (part, chunk of FC features) at a time and
+//    walks its items in a persistent grid-stride sequence.  Each k-step is 16
+//    condensed columns: the 16 gathered X rows (FC features each) and the
+//    16 x W value block are copied global->shared with 16-byte cp.async into
+//    an S-stage ring; the producer cursor runs S-1 steps ahead of the
+//    consumer across item boundaries, so the gather stream never drains.
+//  * The contraction is D[feature, row] += X^T[feature, col] * V[col, row]:
+//    M = 16 features, N = 8 window rows, K = 16 columns, so the sparse block
+//    is the dense B operand and the gathered rows are A.  ldmatrix.trans
+//    turns the row-major gathered X tile into the A fragment; the value tile
+//    feeds B through a plain ldmatrix.  fp32 accumulators stay in registers.
+//    (The reference uses m16n8k8 with fp16 accumulation; this accumulates in
+//    fp32.)  Shared rows are XOR-swizzled per 16-byte chunk so both ldmatrix
+//    forms are bank-conflict free.
+//  * TF32 runs m16n8k8 as a 3xTF32 split (hi*hi + hi*lo + lo*hi), which gives
+//    fp32-level accuracy at no cost on a gather-bound kernel.
+//  * Output: a part of an unsplit window stores its whole W-row tile with
+//    plain stores; parts of split windows add with red.global.add.f32.  A
+//    small pre-pass zeroes only rows that no unsplit part writes (split
+//    windows, windows without parts, trailing rows), so Y needs no memset.
+#include "att_common.cuh"
+
+#include <mutex>
+
+namespace att {
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kThreads = kWarps * 32;
+constexpr int kStages = 4;
+
+struct PartInfo {
+    int start, nreal, nsteps;
+};
+
+__device__ __forceinline__ PartInfo part_info(const int32_t *__restrict__ rowptr, int64_t p) {
+    PartInfo pi;
+    pi.start = __ldg(rowptr + 2 * p);
+    int e = __ldg(rowptr + 2 * p + 1);
+    pi.nreal = e > pi.start ? e - pi.start : 0;
+    pi.nsteps = (pi.nreal + 15) >> 4;
+    return pi;
+}
+
+// XOR swizzle of the 16-byte chunk index within a shared row of `row_bytes`
+template <int ROW_BYTES>
+__device__ __forceinline__ int swz(int r) {
+    if constexpr (ROW_BYTES >= 128) return r & 7;
+    else return (r >> 1) & 3;  // 64-byte rows: two rows share a 128-byte bank window
+}
+
+// ---------------------------------------------------------------------------
+// 16-bit operand kernel (fp16 / bf16 values and features)
+// ---------------------------------------------------------------------------
+template <typename T, int W, int FC, int WIDE>
+struct Cfg16 {
+    static constexpr int XROW = FC * 2;                 // bytes per gathered row in smem
+    static constexpr int XSTAGE = 16 * XROW;            // 16 rows per k-step
+    static constexpr int VSTAGE = 16 * W * 2;           // 16 cols x W rows
+    static constexpr int STAGE = XSTAGE + VSTAGE;
+    static constexpr int WARP_SMEM = kStages * STAGE;
+    static constexpr int SMEM = kWarps * WARP_SMEM;
+    static constexpr int CPR = FC / 8;                  // 16-byte chunks per row
+    static constexpr int RPP = 32 / CPR;                // rows per warp pass
+    static constexpr int MT = FC / 16;                  // m16 tiles
+    static constexpr int NT = W / 8;                    // n8 tiles
+    static constexpr int VCH = VSTAGE / 16;             // value chunks per step
+};
+
+template <typename T, int W, int FC, int WIDE>
+__global__ void __launch_bounds__(kThreads) k_spmm16(
+    const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+    const T *__restrict__ val, const int32_t *__restrict__ win,
+    const int32_t *__restrict__ atomic, int64_t n_parts, const T *__restrict__ X, int64_t n_x,
+    int64_t F, int64_t ldx, float *__restrict__ Y, int64_t m_out, int64_t ldy, int n_chunks,
+    int32_t *__restrict__ err) {
+    using C = Cfg16<T, W, FC, WIDE>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
+    const int64_t n_items = n_parts * n_chunks;
+    const int64_t stride = (int64_t)gridDim.x * kWarps;
+    const int gid = lane >> 2, tig = lane & 3;
+
+    // ---- producer cursor ----
+    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    int p_step = 0;
+    PartInfo p_pi = {0, 0, 0};
+    int p_fc = 0;
+    auto p_load = [&]() {
+        while (p_item < n_items) {
+            int64_t part = p_item / n_chunks;
+            p_fc = (int)(p_item - part * n_chunks);
+            p_pi = part_info(rowptr, part);
+            p_step = 0;
+            if (p_pi.nsteps > 0) return;
+            p_item += stride;
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * C::STAGE;
+        const uint32_t vs = xs + C::XSTAGE;
+        const int c0 = p_step * 16;
+        int myc = -1;
+        if (c0 + (lane & 15) < p_pi.nreal) myc = __ldg(col + p_pi.start + c0 + (lane & 15));
+        const int64_t fbase = (int64_t)p_fc * FC;
+#pragma unroll
+        for (int i = 0; i < 16 / C::RPP; ++i) {
+            const int r = i * C::RPP + lane / C::CPR;
+            const int ch = lane % C::CPR;
+            const int cidx = __shfl_sync(0xffffffffu, myc, r);
+            const int64_t f = fbase + ch * 8;
+            bool ok = cidx >= 0 && f < F;
+            if (cidx >= n_x || cidx < -1) {
+                if (err) atomicOr(err, 1);
+                ok = false;
+            }
+            const T *src = ok ? X + (int64_t)cidx * ldx + f : X;
+            cp_async16(xs + r * C::XROW + ((ch ^ swz<C::XROW>(r)) << 4), src, ok ? 16 : 0);
+        }
+#pragma unroll
+        for (int q = lane; q < C::VCH; q += 32) {
+            const int e = q * 8;                       // element offset within the step's block run
+            const int blk = e / (W * WIDE);
+            const bool ok = c0 + blk * WIDE < p_pi.nreal;
+            const T *src = val + ((int64_t)(p_pi.start + c0) * W + e);
+            cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
+        }
+    };
+    auto p_advance = [&]() {
+        if (++p_step >= p_pi.nsteps) {
+            p_item += stride;
+            p_load();
+        }
+    };
+
+    p_load();
+#pragma unroll
+    for (int s = 0; s < kStages - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+        cp_async_commit();
+    }
+
+    // ---- consumer ----
+    float acc[C::MT][C::NT][4];
+#pragma unroll
+    for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
+
+    int cstage = 0, pstage = kStages - 1;
+    for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const int64_t part = c_item / n_chunks;
+        const int fc = (int)(c_item - part * n_chunks);
+        const PartInfo pi = part_info(rowptr, part);
+        for (int step = 0; step < pi.nsteps; ++step) {
+            cp_async_wait<kStages - 2>();
+            __syncwarp();
+            const uint32_t xs = sbase + cstage * C::STAGE;
+            const uint32_t vs = xs + C::XSTAGE;
+            // B fragments: value tile rows = window rows, 8 columns per matrix
+            uint32_t b[C::NT][2];
+            {
+                const int q = lane >> 3, rr = lane & 7;
+                if constexpr (C::NT == 2) {
+                    const int kb = q & 1, r = (q >> 1) * 8 + rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x4(vs + e * 2, b[0][0], b[0][1], b[1][0], b[1][1]);
+                } else {
+                    const int kb = q & 1, r = rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x2(vs + e * 2, b[0][0], b[0][1]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int q = lane >> 3, rr = lane & 7;
+                const int k = (q >> 1) * 8 + rr;
+                const int ch = 2 * j + (q & 1);
+                uint32_t a[4];
+                ldsm_x4_trans(xs + k * C::XROW + ((ch ^ swz<C::XROW>(k)) << 4), a[0], a[1], a[2],
+                              a[3]);
+#pragma unroll
+                for (int t = 0; t < C::NT; ++t) mma_16816<T>(acc[j][t], a, b[t][0], b[t][1]);
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                issue(pstage);
+                p_advance();
+            }
+            cp_async_commit();
+            cstage = cstage + 1 == kStages ? 0 : cstage + 1;
+            pstage = pstage + 1 == kStages ? 0 : pstage + 1;
+        }
+        // ---- epilogue: the W x FC tile of this part ----
+        const int wrow = __ldg(win + part);
+        const bool add = __ldg(atomic + part) != 0;
+        const int64_t f0 = (int64_t)fc * FC;
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) {
+            const int64_t r0 = (int64_t)wrow * W + t * 8 + 2 * tig;
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int64_t fa = f0 + 16 * j + gid;
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int64_t r = r0 + (h & 1);
+                    const int64_t f = fa + (h >> 1) * 8;
+                    if (r >= 0 && r < m_out && f < F) {
+                        float *dst = Y + r * ldy + f;
+                        if (add) red_add_f32(dst, acc[j][t][h]);
+                        else *dst = acc[j][t][h];
+                    }
+                    acc[j][t][h] = 0.f;
+                }
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// fp32 operand kernel: 3xTF32 m16n8k8
+// ---------------------------------------------------------------------------
+template <int W, int FC, int WIDE>
+struct CfgTF32 {
+    static constexpr int XROW = FC * 4;
+    static constexpr int XSTAGE = 16 * XROW;
+    static constexpr int VSTAGE = 16 * W * 4;
+    static constexpr int STAGE = XSTAGE + VSTAGE;
+    static constexpr int WARP_SMEM = kStages * STAGE;
+    static constexpr int SMEM = kWarps * WARP_SMEM;
+    static constexpr int CPR = FC / 4;
+    static constexpr int RPP = 32 / CPR;
+    static constexpr int MT = FC / 16;
+    static constexpr int NT = W / 8;
+    static constexpr int VCH = VSTAGE / 16;
+};
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
+    hi = f32_to_tf32(x);
+    lo = f32_to_tf32(x - __uint_as_float(hi));
+}
+
+template <int W, int FC, int WIDE>
+__global__ void __launch_bounds__(kThreads) k_spmm_tf32(
+    const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+    const float *__restrict__ val, const int32_t *__restrict__ win,
+    const int32_t *__restrict__ atomic, int64_t n_parts, const float *__restrict__ X, int64_t n_x,
+    int64_t F, int64_t ldx, float *__restrict__ Y, int64_t m_out, int64_t ldy, int n_chunks,
+    int32_t *__restrict__ err) {
+    using C = CfgTF32<W, FC, WIDE>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
+    const unsigned char *sgen = smem + warp * C::WARP_SMEM;
+    const int64_t n_items = n_parts * n_chunks;
+    const int64_t stride = (int64_t)gridDim.x * kWarps;
+    const int gid = lane >> 2, tig = lane & 3;
+
+    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    int p_step = 0, p_fc = 0;
+    PartInfo p_pi = {0, 0, 0};
+    auto p_load = [&]() {
+        while (p_item < n_items) {
+            int64_t part = p_item / n_chunks;
+            p_fc = (int)(p_item - part * n_chunks);
+            p_pi = part_info(rowptr, part);
+            p_step = 0;
+            if (p_pi.nsteps > 0) return;
+            p_item += stride;
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * C::STAGE;
+        const uint32_t vs = xs + C::XSTAGE;
+        const int c0 = p_step * 16;
+        int myc = -1;
+        if (c0 + (lane & 15) < p_pi.nreal) myc = __ldg(col + p_pi.start + c0 + (lane & 15));
+        const int64_t fbase = (int64_t)p_fc * FC;
+#pragma unroll
+        for (int i = 0; i < 16 / C::RPP; ++i) {
+            const int r = i * C::RPP + lane / C::CPR;
+            const int ch = lane % C::CPR;
+            const int cidx = __shfl_sync(0xffffffffu, myc, r);
+            const int64_t f = fbase + ch * 4;
+            bool ok = cidx >= 0 && f < F;
+            if (cidx >= n_x || cidx < -1) {
+                if (err) atomicOr(err, 1);
+                ok = false;
+            }
+            const float *src = ok ? X + (int64_t)cidx * ldx + f : X;
+            cp_async16(xs + r * C::XROW + ((ch ^ ((r & 3) << 1)) << 4), src, ok ? 16 : 0);
+        }
+#pragma unroll
+        for (int q = lane; q < C::VCH; q += 32) {
+            const int e = q * 4;
+            const int blk = e / (W * WIDE);
+            const bool ok = c0 + blk * WIDE < p_pi.nreal;
+            const float *src = val + ((int64_t)(p_pi.start + c0) * W + e);
+            cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
+        }
+    };
+    auto p_advance = [&]() {
+        if (++p_step >= p_pi.nsteps) {
+            p_item += stride;
+            p_load();
+        }
+    };
+
+    p_load();
+#pragma unroll
+    for (int s = 0; s < kStages - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+        cp_async_commit();
+    }
+
+    float acc[C::MT][C::NT][4];
+#pragma unroll
+    for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
+
+    int cstage = 0, pstage = kStages - 1;
+    for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const int64_t part = c_item / n_chunks;
+        const int fc = (int)(c_item - part * n_chunks);
+        const PartInfo pi = part_info(rowptr, part);
+        for (int step = 0; step < pi.nsteps; ++step) {
+            cp_async_wait<kStages - 2>();
+            __syncwarp();
+            const float *xsg = (const float *)(sgen + cstage * C::STAGE);
+            const float *vsg = (const float *)(sgen + cstage * C::STAGE + C::XSTAGE);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {  // two k8 steps per 16-column stage
+                uint32_t bh[C::NT][2], bl[C::NT][2];
+#pragma unroll
+                for (int t = 0; t < C::NT; ++t) {
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int c = 8 * h + tig + 4 * u;
+                        const int r = t * 8 + gid;
+                        const float v = vsg[(c / WIDE) * W * WIDE + r * WIDE + c % WIDE];
+                        split_tf32(v, bh[t][u], bl[t][u]);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < C::MT; ++j) {
+                    uint32_t ah[4], al[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int k = 8 * h + tig + ((u >> 1) << 2);
+                        const int f = 16 * j + gid + ((u & 1) << 3);
+                        const int ch = f >> 2;
+                        const float x = xsg[k * FC + (((ch ^ ((k & 3) << 1))) << 2) + (f & 3)];
+                        split_tf32(x, ah[u], al[u]);
+                    }
+#pragma unroll
+                    for (int t = 0; t < C::NT; ++t) {
+                        mma_1688_tf32(acc[j][t], al[0], al[1], al[2], al[3], bh[t][0], bh[t][1]);
+                        mma_1688_tf32(acc[j][t], ah[0], ah[1], ah[2], ah[3], bl[t][0], bl[t][1]);
+                        mma_1688_tf32(acc[j][t], ah[0], ah[1], ah[2], ah[3], bh[t][0], bh[t][1]);
+                    }
+                }
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                issue(pstage);
+                p_advance();
+            }
+            cp_async_commit();
+            cstage = cstage + 1 == kStages ? 0 : cstage + 1;
+            pstage = pstage + 1 == kStages ? 0 : pstage + 1;
+        }
+        const int wrow = __ldg(win + part);
+        const bool add = __ldg(atomic + part) != 0;
+        const int64_t f0 = (int64_t)fc * FC;
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) {
+            const int64_t r0 = (int64_t)wrow * W + t * 8 + 2 * tig;
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int64_t fa = f0 + 16 * j + gid;
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int64_t r = r0 + (h & 1);
+                    const int64_t f = fa + (h >> 1) * 8;
+                    if (r >= 0 && r < m_out && f < F) {
+                        float *dst = Y + r * ldy + f;
+                        if (add) red_add_f32(dst, acc[j][t][h]);
+                        else *dst = acc[j][t][h];
+                    }
+                    acc[j][t][h] = 0.f;
+                }
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// Zero the output rows that no unsplit part writes: rows of split windows,
+// of windows without parts and rows past the last window.  One warp per window.
+__global__ void k_zero_uncovered(const int32_t *__restrict__ win, const int32_t *__restrict__ atomic,
+                                 int64_t n_parts, int W, float *__restrict__ Y, int64_t m_out,
+                                 int64_t F, int64_t ldy) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_w = (m_out + W - 1) / W;
+    if (w >= n_w) return;
+    int64_t lo = 0, hi = n_parts;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (__ldg(win + mid) < w) lo = mid + 1; else hi = mid;
+    }
+    const bool covered = lo < n_parts && __ldg(win + lo) == w && __ldg(atomic + lo) == 0;
+    if (covered) return;
+    const int64_t r1 = (w + 1) * W < m_out ? (w + 1) * W : m_out;
+    for (int64_t r = w * W; r < r1; ++r)
+        for (int64_t f = lane; f < F; f += 32) Y[r * ldy + f] = 0.f;
+}
+
+template <typename K>
+int occupancy_grid(K kernel, int smem, int64_t items) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    int64_t want = (items + kWarps - 1) / kWarps;
+    int64_t cap = (int64_t)sm_count() * per_sm;
+    return (int)(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+template <typename K>
+int prepare(K kernel, int smem) {
+    // opt in to large dynamic shared memory once per kernel instantiation
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return cuda_status(e, "cudaFuncSetAttribute");
+}
+
+template <typename T, int W, int FC, int WIDE>
+int launch16(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+             const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
+             int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err, cudaStream_t st) {
+    using C = Cfg16<T, W, FC, WIDE>;
+    auto kernel = k_spmm16<T, W, FC, WIDE>;
+    static std::once_flag once;
+    static int prep = ATT_OK;
+    std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+    if (prep != ATT_OK) return prep;
+    const int n_chunks = (int)((F + FC - 1) / FC);
+    const int64_t items = n_parts * n_chunks;
+    if (items == 0) return ATT_OK;
+    const int grid = occupancy_grid(kernel, C::SMEM, items);
+    kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const T *)val, win, atomic, n_parts,
+                                            (const T *)X, n_x, F, ldx, Y, m_out, ldy, n_chunks,
+                                            err);
+    return launch_status("k_spmm16");
+}
+
+template <int W, int FC, int WIDE>
+int launch_tf32(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+                const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
+                int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err, cudaStream_t st) {
+    using C = CfgTF32<W, FC, WIDE>;
+    auto kernel = k_spmm_tf32<W, FC, WIDE>;
+    static std::once_flag once;
+    static int prep = ATT_OK;
+    std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+    if (prep != ATT_OK) return prep;
+    const int n_chunks = (int)((F + FC - 1) / FC);
+    const int64_t items = n_parts * n_chunks;
+    if (items == 0) return ATT_OK;
+    const int grid = occupancy_grid(kernel, C::SMEM, items);
+    kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const float *)val, win, atomic, n_parts,
+                                            (const float *)X, n_x, F, ldx, Y, m_out, ldy, n_chunks,
+                                            err);
+    return launch_status("k_spmm_tf32");
+}
+
+template <typename T, int W, int WIDE>
+int dispatch_fc16(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+                  const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
+                  int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err,
+                  cudaStream_t st) {
+    if (F <= 32)
+        return launch16<T, W, 32, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
+                                        m_out, ldy, err, st);
+    if (F <= 64)
+        return launch16<T, W, 64, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
+                                        m_out, ldy, err, st);
+    return launch16<T, W, 128, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
+                                     m_out, ldy, err, st);
+}
+
+template <int W, int WIDE>
+int dispatch_fc32(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+                  const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
+                  int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err,
+                  cudaStream_t st) {
+    if (F <= 32)
+        return launch_tf32<W, 32, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
+                                        m_out, ldy, err, st);
+    return launch_tf32<W, 64, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
+                                    m_out, ldy, err, st);
+}
+
+}  // namespace
+}  // namespace att
+
+using namespace att;
+
+extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *val, int val_dtype,
+                        const int32_t *window_of_part, const int32_t *atomic, int64_t n_parts,
+                        const void *X, int x_dtype, const float *x_scale, int64_t n_x_rows,
+                        int64_t F, int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int window,
+                        int wide, int32_t *err_flag, void *stream) {
+    clear_error();
+    ATT_CHECK(n_parts >= 0 && m_out >= 0 && F >= 0 && n_x_rows >= 0, ATT_ERR_INVALID,
+              "negative size");
+    ATT_CHECK(window == 8 || window == 16, ATT_ERR_UNSUPPORTED, "window must be 8 or 16, got %d",
+              window);
+    ATT_CHECK(m_out == 0 || F == 0 || Y != nullptr, ATT_ERR_INVALID, "Y is null");
+    ATT_CHECK(ldy >= F, ATT_ERR_INVALID, "ldy %lld < F %lld", (long long)ldy, (long long)F);
+    ATT_CHECK(n_parts == 0 || (rowptr && col && val && window_of_part && atomic && X),
+              ATT_ERR_INVALID, "null format or X pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (m_out == 0 || F == 0) return ATT_OK;
+    int s = ATT_OK;
+    {
+        int64_t threads = (m_out + window - 1) / window * 32;
+        k_zero_uncovered<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+            window_of_part, atomic, n_parts, window, Y, m_out, F, ldy);
+        s = launch_status("k_zero_uncovered");
+        if (s != ATT_OK) return s;
+    }
+    if (n_parts == 0) return ATT_OK;
+    const bool is16 = (val_dtype == ATT_F16 && x_dtype == ATT_F16) ||
+                      (val_dtype == ATT_BF16 && x_dtype == ATT_BF16);
+    if (is16) {
+        ATT_CHECK(wide == 8 || wide == 16, ATT_ERR_UNSUPPORTED,
+                  "16-bit values need wide 8 or 16, got %d", wide);
+        ATT_CHECK(F % 8 == 0 && ldx % 8 == 0 && ((uintptr_t)X & 15) == 0 && ((uintptr_t)val & 15) == 0,
+                  ATT_ERR_UNSUPPORTED,
+                  "16-bit SpMM needs F and ldx multiples of 8 and 16-byte aligned X and values");
+        ATT_CHECK(ldx >= F, ATT_ERR_INVALID, "ldx < F");
+#define ATT_SPMM16(T, Wv, WIDEv)                                                             \
+    return dispatch_fc16<T, Wv, WIDEv>(rowptr, col, val, window_of_part, atomic, n_parts, X, \
+                                       n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st)
+        if (val_dtype == ATT_F16) {
+            if (window == 8 && wide == 8) ATT_SPMM16(__half, 8, 8);
+            if (window == 8 && wide == 16) ATT_SPMM16(__half, 8, 16);
+            if (window == 16 && wide == 8) ATT_SPMM16(__half, 16, 8);
+            ATT_SPMM16(__half, 16, 16);
+        } else {
+            if (window == 8 && wide == 8) ATT_SPMM16(__nv_bfloat16, 8, 8);
+            if (window == 8 && wide == 16) ATT_SPMM16(__nv_bfloat16, 8, 16);
+            if (window == 16 && wide == 8) ATT_SPMM16(__nv_bfloat16, 16, 8);
+            ATT_SPMM16(__nv_bfloat16, 16, 16);
+        }
+#undef ATT_SPMM16
+    }
+    if (val_dtype == ATT_F32 && x_dtype == ATT_F32) {
+        ATT_CHECK(wide == 4 || wide == 8, ATT_ERR_UNSUPPORTED, "fp32 values need wide 4 or 8, got %d",
+                  wide);
+        ATT_CHECK(F % 4 == 0 && ldx % 4 == 0 && ((uintptr_t)X & 15) == 0 && ((uintptr_t)val & 15) == 0,
+                  ATT_ERR_UNSUPPORTED,
+                  "fp32 SpMM needs F and ldx multiples of 4 and 16-byte aligned X and values");
+        ATT_CHECK(ldx >= F, ATT_ERR_INVALID, "ldx < F");
+        if (window == 8 && wide == 4)
+            return dispatch_fc32<8, 4>(rowptr, col, val, window_of_part, atomic, n_parts, X,
+                                       n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st);
+        if (window == 8 && wide == 8)
+            return dispatch_fc32<8, 8>(rowptr, col, val, window_of_part, atomic, n_parts, X,
+                                       n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st);
+        if (window == 16 && wide == 4)
+            return dispatch_fc32<16, 4>(rowptr, col, val, window_of_part, atomic, n_parts, X,
+                                        n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st);
+        return dispatch_fc32<16, 8>(rowptr, col, val, window_of_part, atomic, n_parts, X, n_x_rows,
+                                    F, ldx, Y, m_out, ldy, err_flag, st);
+    }
+    (void)x_scale;
+    set_error("unsupported (val_dtype=%d, x_dtype=%d) combination", val_dtype, x_dtype);
+    return ATT_ERR_UNSUPPORTED;
+}

@@ -1,0 +1,393 @@
+"""Benchmark of the ATT sparse hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {ours,reference}]
+                    [--workload NAME]
+
+Workloads (synthetic seeded Chung-Lu graphs standing in for the reference's
+datasets, which are not available):
+
+  spmm_products_fp16   blocked SpMM Y = A_hat X, N = 2,449,029 nodes (ogbn-products
+                       shape), gamma 2.2, mean degree 25 (~62M edges) + self-loops,
+                       GCN-normalised fp16 values, X [N, 128] fp16 U[-1,1] with 100
+                       real dims and 28 zero dims, reference block format
+                       (8-row windows, 8-wide blocks, partSize 32), fp32 output.
+
+One step = one pass of the hot path over the whole graph.  ``value`` is
+algorithmic GB/s (bytes defined in the roofline note below) with inputs
+resident in HBM; every input (format 1.2 GB, X 0.6 GB) is larger than L2, so
+no flush is needed between steps.  ``e2e`` times the same step through the
+reference-facing drop-in (``SpMM_sr_bcrs.forward_fp16_gnn``) with X copied
+from pinned host memory and Y copied back every step.
+
+Multi-GPU: the path runs as independent replicas (one whole graph per GPU,
+weak scaling; no collective on the data path).
+
+``--impl reference`` times the reference's CPU path for this op, restated in
+the oracle (torch.sparse CSR SpMM in fp32 on all host cores), on a bounded
+sample of rows of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "SpMM/SDDMM HBM GB/s (% roofline); GAT step ms; serve p50/p99 vs plain"
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+class SpmmProducts:
+    """Blocked FP16 SpMM on the 2.45M-node power-law graph."""
+    name = "spmm_products_fp16"
+    unit = "GB/s"
+    N, MEAN_DEG, GAMMA, SEED, F, F_REAL = 2_449_029, 25, 2.2, 2, 128, 100
+
+    def __init__(self, device, scale=1.0):
+        import torch
+        from att_gb300 import graphs, ops
+        self.torch = torch
+        n = int(self.N * scale)
+        self.n = n
+        rp, col = graphs.chung_lu(n, self.MEAN_DEG, self.GAMMA, self.SEED, device=device)
+        rp = graphs.pad_rows(rp, 8)
+        self.rowptr, self.colidx = rp, col
+        deg = graphs.gcn_degree(rp, torch.float16)
+        deg = torch.where(torch.isfinite(deg), deg, torch.zeros_like(deg))
+        self.deg = deg
+        self.fmt = ops.block_convert(rp, col, deg, window=8, wide=8, part=32)
+        g = torch.Generator(device=device)
+        g.manual_seed(self.SEED)
+        X = torch.rand(n, self.F, generator=g, device=device, dtype=torch.float32) * 2 - 1
+        X[:, self.F_REAL:] = 0
+        self.X = X.half()
+        self.Y = torch.empty(n, self.F, device=device, dtype=torch.float32)
+        f = self.fmt
+        real = (f.rowptr[1::2] - f.rowptr[0:-1:2]).sum().item()
+        self.nnz = int(col.shape[0])
+        self.U = int(real)  # distinct (8-row window, column) pairs = gathered X rows
+        F = self.F
+        self.bytes_alg = 4 * (n + 1) + self.nnz * (4 + 2) + self.U * F * 2 + n * F * 4
+        self.flops = 2 * self.nnz * F
+        self.launches_per_step = 2  # k_zero_uncovered + k_spmm16
+        self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz,
+                       "features": F, "real_features": self.F_REAL, "gamma": self.GAMMA,
+                       "mean_degree": self.MEAN_DEG, "seed": self.SEED,
+                       "format": "window 8, wide 8, partSize 32",
+                       "parts": f.n_parts, "condensed_cols": f.n_condensed,
+                       "gathered_rows_U8": self.U, "x_dtype": "fp16", "y_dtype": "fp32",
+                       "l2": "inputs larger than L2 (no flush)"}
+
+    def step(self):
+        from att_gb300 import ops
+        f = self.fmt
+        ops.spmm(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, self.X, self.n, out=self.Y)
+
+    # end to end through the reference-facing drop-in, host buffers
+    def e2e_setup(self):
+        torch = self.torch
+        self.Xh = self.X.cpu().pin_memory()
+        self.Yh = torch.empty(self.n, self.F, dtype=torch.float32).pin_memory()
+        from att_gb300.compat import SpMM_sr_bcrs
+        self._mod = SpMM_sr_bcrs
+        self.h2d = self.Xh.numel() * 2
+        self.d2h = self.Yh.numel() * 4
+
+    def e2e_step(self):
+        f = self.fmt
+        Xd = self.Xh.to("cuda", non_blocking=True)
+        Y = self._mod.forward_fp16_gnn(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, Xd,
+                                       self.rowptr.shape[0] - 1, self.F, self.n)[0]
+        self.Yh.copy_(Y, non_blocking=True)
+
+    def check(self):
+        """Size-independent property at full size: A_hat applied to a constant
+        column equals the per-row sum of the block values (checksum of checksums)."""
+        torch = self.torch
+        from att_gb300 import ops
+        ones = torch.zeros(self.n, 8, device=self.X.device, dtype=torch.float16)
+        ones[:, 0] = 1
+        f = self.fmt
+        Y1 = ops.spmm(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, ones, self.n)[:, 0]
+        rows = torch.repeat_interleave(torch.arange(self.rowptr.shape[0] - 1, device=self.X.device),
+                                       (self.rowptr[1:] - self.rowptr[:-1]).long())
+        ev = (self.deg[rows].float() * self.deg[self.colidx.long()].float()).half().float()
+        rs = torch.zeros(self.rowptr.shape[0] - 1, device=self.X.device).index_add_(0, rows, ev)
+        err = ((Y1 - rs[: self.n]).abs().max() / rs.abs().max().clamp_min(1e-30)).item()
+        return err
+
+    # CPU baseline: the oracle's restatement of the reference's CPU path
+    def cpu_sample(self, max_rows):
+        """CSR fp32 of the first `max_rows` rows (host), and the algorithmic bytes."""
+        torch = self.torch
+        rows = min(max_rows, self.n)
+        rp = self.rowptr[: rows + 1].cpu().long()
+        col = self.colidx[: int(rp[-1])].cpu().long()
+        ridx = torch.repeat_interleave(torch.arange(rows), rp[1:] - rp[:-1])
+        d = self.deg.cpu().float()
+        vals = (d[ridx] * d[col]).half().float()
+        X = self.X.float().cpu()
+        f = self.fmt
+        wins = f.window_of_part.cpu()
+        rr = f.rowptr.cpu()
+        sel = wins < (rows // 8)
+        U = int((rr[1::2] - rr[0:-1:2])[sel].sum())
+        nnz = int(col.shape[0])
+        b = 4 * (rows + 1) + nnz * (4 + 2) + U * self.F * 2 + rows * self.F * 4
+        return rp, col, vals, X, rows, b
+
+
+WORKLOADS = {SpmmProducts.name: SpmmProducts}
+DEFAULT_WORKLOAD = SpmmProducts.name
+
+
+# ---------------------------------------------------------------------------
+def _env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def cpu_baseline(wl, budget_s=12.0):
+    """Time the oracle (torch.sparse CSR SpMM, fp32, all host threads) on a
+    bounded row sample; returns the cpu_baseline dict."""
+    import torch
+    from oracle import oracle as orc
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    rows = max(8, wl.n // 64)
+    rp, col, vals, X, rows, b = wl.cpu_sample(rows)
+    A = orc.csr_fp32(rp, col, vals, X.shape[0])
+    t0 = time.perf_counter()
+    orc.spmm_cpu_fp32(A, X)
+    one = time.perf_counter() - t0
+    reps = max(3, min(50, int(budget_s / max(one, 1e-3))))
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        orc.spmm_cpu_fp32(A, X)
+        ts.append(time.perf_counter() - t0)
+    ts.sort()
+    med = ts[len(ts) // 2]
+    return {"value": b / med / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "first %d rows of the same graph (%d edges), torch.sparse CSR fp32 SpMM x "
+                      "[N,%d], median of %d runs" % (rows, int(col.shape[0]), X.shape[1], reps),
+            "ms_per_sample": med * 1e3}
+
+
+def run_reference(args):
+    rank, local, world = _env_rank()
+    if rank != 0:
+        return 0
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t_setup = time.time()
+    wl = WORKLOADS[args.workload](dev)
+    base = cpu_baseline(wl, budget_s=max(3.0, 20.0 / max(1, args.steps + args.warmup)))
+    line = {"metric": METRIC, "impl": "reference", "value": base["value"], "unit": wl.unit,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": base["ms_per_sample"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(wl.config, note="reference CPU path restated by the oracle "
+                                           "(no CPU SpMM ships in the reference)"),
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": base["value"], "unit": wl.unit, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "setup_s": time.time() - t_setup}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    rank, local, world = _env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from att_gb300 import builder
+    if rank == 0:
+        builder.build()
+    if world > 1:
+        dist.barrier()
+    from att_gb300 import _lib
+    _lib.load()
+
+    wl = WORKLOADS[args.workload]("cuda")
+    check_err = wl.check()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        wl.step()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    t_all0 = torch.cuda.Event(enable_timing=True)
+    t_all1 = torch.cuda.Event(enable_timing=True)
+    t_all0.record(stream)
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        wl.step()
+        ev[k][1].record(stream)
+    t_all1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    total_ms = t_all0.elapsed_time(t_all1)
+    per_launch = sorted(a.elapsed_time(b) for a, b in ev)
+    avg_launch_ms = sum(per_launch) / len(per_launch)
+    t_max = torch.tensor([total_ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    total_ms = float(t_max.item())
+    ms_per_step = total_ms / args.steps
+    value = world * wl.bytes_alg / (ms_per_step * 1e-3) / 1e9
+
+    # end to end through the drop-in with host buffers
+    wl.e2e_setup()
+    for _ in range(2):
+        wl.e2e_step()
+    torch.cuda.synchronize()
+    e_steps = max(3, min(args.steps, 20))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        wl.e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e_steps
+    e2e_ms_t = torch.tensor([e2e_ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(e2e_ms_t, op=dist.ReduceOp.MAX)
+    e2e_ms = float(e2e_ms_t.item())
+
+    peak, peak_kind = peaks()
+    achieved = wl.bytes_alg / (avg_launch_ms * 1e-3) / 1e9
+    line = None
+    if rank == 0:
+        base = None
+        if not args.no_cpu_baseline:
+            base = cpu_baseline(wl)
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                "kernel": "att_spmm (k_zero_uncovered + k_spmm16), avg of %d launches" % args.steps,
+                "bytes_per_launch": wl.bytes_alg}
+        line = {"metric": METRIC, "value": value, "unit": wl.unit, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f16", "data": "synthetic", "config": dict(wl.config),
+                "roofline": roof,
+                "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+                                 if base else None),
+                "e2e": {"value": world * wl.bytes_alg / (e2e_ms * 1e-3) / 1e9, "unit": wl.unit,
+                        "h2d_bytes_per_step": wl.h2d, "d2h_bytes_per_step": wl.d2h,
+                        "ms_per_step": e2e_ms, "api": "SpMM_sr_bcrs.forward_fp16_gnn"},
+                "gpu_launches": wl.launches_per_step * args.steps,
+                "clocks": clocks,
+                "gflops": world * wl.flops / (ms_per_step * 1e-3) / 1e9,
+                "check_rel_err": check_err,
+                "launch_ms_p50": per_launch[len(per_launch) // 2]}
+        print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,145 @@
+/*
+ * att_gb300.h -- C ABI of the GB300 (sm_103a) ATT sparse hot path.
+ *
+ * Every entry point takes plain device pointers, element counts and a CUDA
+ * stream (passed as `void *`, a cudaStream_t; NULL = legacy default stream),
+ * launches asynchronously on that stream and returns an att_status.  No entry
+ * point allocates device memory: outputs and workspaces are the caller's.
+ * Only the two-phase conversion's plan step synchronises the stream (it has
+ * to return the output sizes to the host).
+ *
+ * Block format ("row-window block-condensed", the reference's layout):
+ *   rows are grouped in windows of W rows; each window's distinct columns are
+ *   listed in ascending order and padded with -1 to a multiple of `wide`;
+ *   the columns of all windows are concatenated (col[n_cols]); the value of
+ *   slot (window row r, condensed column c) sits at
+ *       val[(c - c % wide) * W + r * wide + c % wide]
+ *   (blocks of W x wide, row-major, one block after another).  A window with
+ *   more than `part` blocks is split into parts; part p covers condensed
+ *   columns [rowptr[2p], rowptr[2p+2]), of which [rowptr[2p], rowptr[2p+1])
+ *   are real; window_of_part[p] is its window, atomic[p] = 1 if its window
+ *   was split.  Parts are in ascending window order.
+ *
+ * The reference interfaces each function replaces are cited by file:line of
+ * the reference project.
+ */
+#ifndef ATT_GB300_H
+#define ATT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ATT_API __attribute__((visibility("default")))
+#else
+#define ATT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum att_status {
+    ATT_OK = 0,
+    ATT_ERR_INVALID = 1,     /* bad argument (null pointer, size, dtype, alignment) */
+    ATT_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
+    ATT_ERR_WORKSPACE = 3,   /* workspace smaller than the size query returned */
+    ATT_ERR_UNSUPPORTED = 4, /* valid but not implemented combination */
+    ATT_ERR_OVERFLOW = 5,    /* output would exceed int32 indexing */
+    ATT_ERR_FORMAT = 6       /* device-side check found a malformed input */
+};
+
+/* ---- element types ----------------------------------------------------- */
+enum att_dtype {
+    ATT_F32 = 0,
+    ATT_F16 = 1,
+    ATT_BF16 = 2,
+    ATT_F8E4M3 = 3,
+    ATT_I32 = 4,
+    ATT_NONE = -1
+};
+
+/* Human-readable name of a status. */
+ATT_API const char *att_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+ATT_API const char *att_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+ATT_API int att_version(void);
+
+/* ======================================================================
+ * Conversion: CSR -> row-window block-condensed format, on the GPU.
+ * Replaces Block_sr_bcrs.blockProcess_fp16_balance / _tf32_balance
+ * (gcn/Block_gcn/example.cpp:48-200, :203-348; pybind :353-357) and
+ * ATT_Block[_v3].blockProcess_sddmm_balance_gnn[_trans]
+ * (Block/include/example.h:4-6, called from
+ * end2end_ori/gat_final/mgat_csr/mdataset_fp16.py:57-62) and the GPU
+ * preprocessing ATT_Block_gpu.preprocess_gpu_fs
+ * (end2end_overhead/gat_final/mgat_csr_ov/mdataset_fp16.py:53-58).
+ * Output is bit-identical to the reference's CPU conversion.
+ *
+ * n_rows = rowptr length - 1; column ids must lie in [0, n_cols).
+ * emit_empty = 1 reproduces the tf32 variant (an empty window emits a
+ * (0,0) part), 0 the fp16 variant (empty windows emit nothing).
+ * ====================================================================== */
+
+/* Bytes of device workspace att_block_plan / att_block_fill need. */
+ATT_API size_t att_block_workspace_bytes(int64_t n_rows, int64_t nnz, int64_t n_cols, int window);
+
+/* Phase 1: per-window distinct columns.  Writes the number of parts and of
+ * padded condensed columns to the host pointers; synchronises `stream`. */
+ATT_API int att_block_plan(const int32_t *rowptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                   int64_t n_cols, int window, int wide, int part, int emit_empty,
+                   void *workspace, size_t workspace_bytes,
+                   int64_t *n_parts_out, int64_t *n_condensed_out, void *stream);
+
+/* Phase 2: write the format.  Output sizes: rowptr 2*n_parts+1, col
+ * n_condensed, val / map / map_t n_condensed*window, window_of_part and atomic
+ * n_parts.  Any of val, map, map_t may be NULL to skip it.
+ *   deg (deg_dtype ATT_F16 or ATT_F32, length >= n_cols and >= n_rows) gives
+ *   val = deg[row]*deg[col] computed in fp32 and rounded to val_dtype
+ *   (ATT_F16, ATT_BF16 or ATT_F32); duplicate (row,col) entries overwrite.
+ *   map[slot]   = the last CSR edge id landing in the slot, -1 if empty.
+ *   map_t[slot] = the last CSR edge id of the mirrored edge (col,row), -1 if
+ *                 absent; needs rows sorted by column (checked: status
+ *                 ATT_ERR_FORMAT otherwise).
+ *   edge_slot (may be NULL): for each CSR edge e, the slot index its value
+ *   landed in (the compact per-edge form the GAT kernels consume).
+ * Synchronises `stream` to read the device-side checks. */
+ATT_API int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                   int64_t n_cols, int window, int wide, int part, int emit_empty,
+                   const void *deg, int deg_dtype, const void *workspace, size_t workspace_bytes,
+                   int32_t *out_rowptr, int32_t *out_col, void *out_val, int val_dtype,
+                   int32_t *out_map, int32_t *out_map_t, int32_t *out_edge_slot,
+                   int32_t *out_window, int32_t *out_atomic, void *stream);
+
+/* ======================================================================
+ * Blocked SpMM:  Y[m_out, F] = A_blocks * X   (tensor cores, fp32 accumulate)
+ * Replaces SpMM_sr_bcrs.forward_fp16_gnn / forward_tf32_gnn /
+ * forward_fp16_gnn_acc / forward_tf32_gnn_acc (gcn/SpMM/src/benchmark.cpp:35-75,
+ * :91-130, :259-296, :305-335; kernels gcn/SpMM/src/spmmKernel.cu:158-265,
+ * :959-1075, :2066-2173, :2214-2330; launchers :1693-1765, :2175-2209,
+ * :2332-2366).
+ *
+ *   val_dtype / x_dtype: (ATT_F16, ATT_F16), (ATT_BF16, ATT_BF16),
+ *     (ATT_F32, ATT_F32) [3xTF32 split, fp32-level accuracy], or
+ *     (ATT_F16, ATT_F8E4M3) with x_scale[n_x_rows] fp32 per-row scales
+ *     (X_true[j] = x_scale[j] * X_e4m3[j]).
+ *   X row j at X + j*ldx elements; Y row i at Y + i*ldy elements (fp32).
+ *   Every row of Y in [0, m_out) is written (rows of windows without parts
+ *   are zeroed), so Y needs no prior clearing.
+ *   window: 8 or 16; wide: 8 or 16 for 16-bit values, 4 or 8 for fp32.
+ *   err_flag (device int32, may be NULL): set non-zero if a column id is
+ *   outside [-1, n_x_rows); such columns contribute nothing.
+ * ====================================================================== */
+ATT_API int att_spmm(const int32_t *rowptr, const int32_t *col, const void *val, int val_dtype,
+             const int32_t *window_of_part, const int32_t *atomic, int64_t n_parts,
+             const void *X, int x_dtype, const float *x_scale, int64_t n_x_rows,
+             int64_t F, int64_t ldx, float *Y, int64_t m_out, int64_t ldy,
+             int window, int wide, int32_t *err_flag, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATT_GB300_H */

@@ -1,0 +1,115 @@
+"""GPU conversion vs the reference's outputs (golden) and the C oracle:
+bit-exact on every output array."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle
+from tests._fixture import ROW, COL
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "blocks_golden.npz")
+
+
+def _bits(a):
+    a = np.asarray(a)
+    if a.dtype == np.float16:
+        return a.view(np.uint16)
+    if a.dtype == np.float32:
+        return a.view(np.uint32)
+    return a
+
+
+def _gpu(rowptr, col, deg, W, w, P, emit_empty, **kw):
+    from att_gb300 import ops
+    d = None if deg is None else torch.from_numpy(np.ascontiguousarray(deg))
+    return ops.block_convert(torch.from_numpy(rowptr), torch.from_numpy(col), d, window=W, wide=w,
+                             part=P, emit_empty=emit_empty, **kw)
+
+
+def test_matches_reference_golden(cuda):
+    g = np.load(GOLDEN)
+    for gi in range(int(g["n_graphs"])):
+        rowptr, col = g["g%d_rowptr" % gi], g["g%d_col" % gi]
+        for (W, w, P) in g["configs"]:
+            for kind in ("fp16", "tf32"):
+                deg = g["g%d_deg16" % gi] if kind == "fp16" else g["g%d_deg32" % gi]
+                f = _gpu(rowptr, col, deg, int(W), int(w), int(P), kind == "tf32")
+                key = "g%d_%s_%d_%d_%d" % (gi, kind, W, w, P)
+                got = dict(rowptr=f.rowptr, col=f.col, val=f.val, window=f.window_of_part,
+                           atomic=f.atomic)
+                for name, t in got.items():
+                    assert np.array_equal(_bits(t.cpu().numpy()), _bits(g[key + "_" + name])), \
+                        (key, name)
+
+
+def test_compat_module_returns_reference_tuple(cuda):
+    from att_gb300.compat import Block_sr_bcrs
+    res = Block_sr_bcrs.blockProcess_fp16_balance(torch.from_numpy(ROW), torch.from_numpy(COL),
+                                                  torch.ones(32, dtype=torch.float16), 8, 8, 1)
+    assert len(res) == 5 and all(t.device.type == "cpu" for t in res)
+    assert res[0].tolist() == [0, 8, 8, 11, 16, 21, 24, 32, 32, 35, 40, 45, 48]
+    assert res[3].tolist() == [0, 0, 1, 2, 2, 3]
+    assert res[4].tolist() == [1, 1, 0, 1, 1, 0]
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_random_graphs_vs_oracle_with_maps(cuda, case):
+    from att_gb300 import graphs
+    specs = [
+        dict(n_rows=300, n_cols=300, max_len=12, seed=1),
+        dict(n_rows=517, n_cols=517, max_len=6, seed=2, hub_rows=3, hub_len=450),
+        dict(n_rows=240, n_cols=240, max_len=10, seed=3, empty_frac=0.6),
+        dict(n_rows=129, n_cols=2000, max_len=40, seed=4, dup=True, sort_rows=False),
+        dict(n_rows=64, n_cols=9000, max_len=3, seed=5, hub_rows=4, hub_len=5000),  # > smem cap
+        dict(n_rows=1001, n_cols=1001, max_len=30, seed=6, hub_rows=1, hub_len=1000),
+    ]
+    sp = specs[case]
+    rowptr, col = graphs.random_csr(**sp)
+    n_cols = sp["n_cols"]
+    rng = np.random.default_rng(case)
+    d32 = (1.0 / np.sqrt(rng.integers(1, 50, size=max(n_cols, rowptr.shape[0])))).astype(np.float32)
+    d16 = d32.astype(np.float16)
+    sorted_rows = sp.get("sort_rows", True)
+    for (W, w, P) in ((8, 8, 32), (8, 4, 32), (16, 8, 4), (8, 16, 2), (16, 16, 1)):
+        for deg, emit in ((d16, False), (d32, True)):
+            o = oracle.block_convert(rowptr, col, deg, W, w, P, emit_empty=emit, want_map=True,
+                                     want_trans=sorted_rows)
+            f = _gpu(rowptr, col, deg, W, w, P, emit, want_map=True, want_trans=sorted_rows,
+                     want_edge_slot=True, n_cols=deg.shape[0])
+            for name, t in (("rowptr", f.rowptr), ("col", f.col), ("val", f.val),
+                            ("window", f.window_of_part), ("atomic", f.atomic), ("map", f.map)):
+                assert np.array_equal(_bits(t.cpu().numpy()), _bits(o[name])), (case, W, w, P, name)
+            if sorted_rows:
+                assert np.array_equal(f.map_t.cpu().numpy(), o["map_t"]), (case, W, w, P)
+            # edge_slot inverts the map for the last duplicate of each slot
+            es = f.edge_slot.cpu().numpy()
+            mp = f.map.cpu().numpy()
+            used = es >= 0
+            assert np.all(mp[es[used]] >= np.nonzero(used)[0])
+
+
+def test_unsorted_rows_rejected_for_mirror_map(cuda):
+    from att_gb300 import graphs, _lib
+    rowptr, col = graphs.random_csr(64, 64, 8, seed=9, sort_rows=False)
+    with pytest.raises(_lib.AttError):
+        _gpu(rowptr, col, None, 8, 8, 32, False, want_map=True, want_trans=True)
+
+
+def test_bad_column_rejected(cuda):
+    from att_gb300 import _lib
+    col = COL.copy()
+    col[5] = 40
+    with pytest.raises(_lib.AttError):
+        _gpu(ROW, col, np.ones(32, np.float16), 8, 8, 32, False)
+
+
+def test_empty_graph(cuda):
+    rowptr = np.zeros(17, np.int32)
+    col = np.zeros(0, np.int32)
+    f = _gpu(rowptr, col, np.ones(16, np.float16), 8, 8, 32, False)
+    assert f.n_parts == 0 and f.rowptr.tolist() == [0]
+    f = _gpu(rowptr, col, np.ones(16, np.float32), 8, 4, 32, True)
+    assert f.n_parts == 2 and f.rowptr.tolist() == [0, 0, 0, 0, 0]

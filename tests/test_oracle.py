@@ -1,0 +1,115 @@
+"""The CPU oracle pinned against the reference's own outputs (golden file made
+by tests/golden/make_golden.py from the reference's compiled conversion) and
+against the known answers of the reference's tests."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests._fixture import ROW, COL
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "blocks_golden.npz")
+
+
+def _golden():
+    return np.load(GOLDEN)
+
+
+def test_f16_rounding_matches_numpy():
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.standard_normal(20000).astype(np.float32) * 10.0 ** rng.integers(-9, 5, 20000),
+                         np.array([65504, 65520, 65536, 1e-8, 2 ** -24, 2 ** -25, 3 * 2 ** -26, 0.0, -0.0],
+                                  np.float32)])
+    want = xs.astype(np.float16).view(np.uint16)
+    got = np.array([oracle.f32_to_f16_bits(float(x)) for x in xs], np.uint16)
+    assert np.array_equal(got, want)
+
+
+def test_oracle_matches_reference_golden():
+    g = _golden()
+    n = int(g["n_graphs"])
+    for gi in range(n):
+        rowptr, col = g["g%d_rowptr" % gi], g["g%d_col" % gi]
+        for (W, w, P) in g["configs"]:
+            for kind in ("fp16", "tf32"):
+                deg = g["g%d_deg16" % gi] if kind == "fp16" else g["g%d_deg32" % gi]
+                o = oracle.block_convert(rowptr, col, deg, int(W), int(w), int(P),
+                                         emit_empty=(kind == "tf32"))
+                key = "g%d_%s_%d_%d_%d" % (gi, kind, W, w, P)
+                for name in ("rowptr", "col", "window", "atomic"):
+                    assert np.array_equal(o[name], g[key + "_" + name]), (key, name)
+                ref_val = g[key + "_val"]
+                bits = np.uint16 if kind == "fp16" else np.uint32
+                assert np.array_equal(o["val"].view(bits), ref_val.view(bits)), (key, "val")
+
+
+def test_known_split_of_fixture():
+    # (window, wide, partSize) = (8, 8, 1): every block its own part
+    o = oracle.block_convert(ROW, COL, np.ones(32, np.float16), 8, 8, 1)
+    assert o["rowptr"].tolist() == [0, 8, 8, 11, 16, 21, 24, 32, 32, 35, 40, 45, 48]
+    assert o["window"].tolist() == [0, 0, 1, 2, 2, 3]
+    assert o["atomic"].tolist() == [1, 1, 0, 1, 1, 0]
+
+
+def test_map_semantics_on_fixture():
+    o = oracle.block_convert(ROW, COL, None, 8, 8, 32, want_map=True, want_trans=True)
+    mp, W, w = o["map"], 8, 8
+    rows = oracle.csr_rows(ROW)
+    seen = np.zeros(COL.shape[0], bool)
+    for slot, e in enumerate(mp):
+        if e < 0:
+            continue
+        blk, rem = slot // (W * w), slot % (W * w)
+        r, k = rem // w, rem % w
+        cond = blk * w + k
+        # slot's window row and condensed column hold edge e
+        assert o["col"][cond] == COL[e]
+        assert rows[e] % W == r
+        seen[e] = True
+    assert seen.all()
+
+
+def test_semantic_pins_on_fixture():
+    rng = np.random.default_rng(1)
+    h, n, F = 4, 30, 125
+    rp = ROW[: n + 1]
+    col = COL[: rp[-1]]
+    X = rng.integers(1, 3, size=(h, n, F)).astype(np.float64)
+    out = oracle.sddmm_fp64(rp, col, X, X)
+    assert out[0][0] == X[0][0] @ X[0][1]          # test_sddmm_fp16.py:62
+    assert out[1][1] == X[1][0] @ X[1][2]          # test_sddmm_fp16.py:67
+    a = np.ones((h, 1, F))
+    att = oracle.att_fp64(rp, col, X, a, a)
+    assert att[1][1] == X[1][0] @ a[1][0] + X[1][2] @ a[1][0]   # test_sddmm_tf32_att.py
+    g = rng.integers(1, 5, size=(n, h, 1)).astype(np.float64)
+    ones = oracle.ones_fp64(rp, g)
+    assert ones[0][0] == g[0][0][0] and ones[1][6] == g[1][1][0]  # test_sddmm_fp16_ones.py:62-68
+    vals = np.ones((3, col.shape[0]))
+    rs = oracle.rowsum_fp64(rp, vals, n)
+    assert np.array_equal(rs[0], np.diff(rp).astype(np.float64))  # test_spmm_h_m_ones.py
+
+
+def test_spmm_oracles_agree():
+    from att_gb300 import graphs
+    rp, col = graphs.random_csr(203, 203, 9, seed=3, hub_rows=2, hub_len=150)
+    deg = (1.0 / np.sqrt(np.maximum(np.diff(rp), 1))).astype(np.float16)
+    X = np.random.default_rng(2).uniform(-1, 1, size=(203, 16))
+    for (W, w, P) in ((8, 8, 32), (16, 8, 2), (8, 4, 3)):
+        o = oracle.block_convert(rp, col, deg, W, w, P)
+        a = oracle.spmm_blocks_fp64(o, X, 203, W, w)
+        b = oracle.spmm_csr_fp64(rp[: (203 // W) * W + 1], col[: rp[(203 // W) * W]],
+                                 oracle.gcn_values(rp, col, deg)[: rp[(203 // W) * W]], X, 203)
+        b = np.vstack([b, np.zeros((203 - b.shape[0], 16))])
+        assert np.allclose(a, b, rtol=0, atol=1e-12)
+
+
+def test_graph_generator_hits_edge_count():
+    from att_gb300 import graphs
+    rp, col = graphs.chung_lu(4096, 10, 2.1, seed=0)
+    assert int(rp[-1]) == 4096 * 10 + 4096
+    r = np.asarray(rp)
+    c = np.asarray(col)
+    for i in range(0, 4096, 97):
+        row = c[r[i]:r[i + 1]]
+        assert np.all(np.diff(row) > 0)

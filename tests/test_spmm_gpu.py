@@ -1,0 +1,123 @@
+"""Blocked SpMM on the GPU vs the FP64 oracle.
+
+Tolerances (normwise relative, max|err| / max|ref|): fp16 and bf16 features
+1e-2, fp32 (3xTF32) 1e-4; integer-valued inputs must match exactly, as the
+reference's own test_balance.py demands."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle
+from tests._fixture import ROW, COL
+
+pytestmark = pytest.mark.gpu
+
+TOL = {torch.float16: 1e-2, torch.bfloat16: 1e-2, torch.float32: 1e-4}
+
+
+def _format(rowptr, col, deg, W, w, P, emit=False):
+    from att_gb300 import ops
+    return ops.block_convert(torch.from_numpy(rowptr), torch.from_numpy(col),
+                             torch.from_numpy(deg), window=W, wide=w, part=P, emit_empty=emit)
+
+
+def _ref(rowptr, col, vals, X, m_out, W):
+    n_used = (rowptr.shape[0] - 1) // W * W
+    rp = rowptr[: n_used + 1]
+    Y = oracle.spmm_csr_fp64(rp, col[: rp[-1]], vals[: rp[-1]], X, None)
+    out = np.zeros((m_out, X.shape[1]))
+    k = min(m_out, Y.shape[0])
+    out[:k] = Y[:k]
+    return out
+
+
+def test_reference_balance_test_exact(cuda):
+    """gcn/SpMM/test/mgcn/test_balance.py:20-62: fixture, deg = 1, integer
+    features -> exact."""
+    from att_gb300.compat import Block_sr_bcrs, SpMM_sr_bcrs
+    for dimN in (64, 128, 66, 125):
+        fmt = Block_sr_bcrs.blockProcess_fp16_balance(torch.from_numpy(ROW), torch.from_numpy(COL),
+                                                      torch.ones(32, dtype=torch.float16), 8, 8, 32)
+        rhs = torch.randint(1, 3, (30, dimN)).half()
+        fmt = [t.cuda() for t in fmt]
+        Y = SpMM_sr_bcrs.forward_fp16_gnn(fmt[0], fmt[1], fmt[2], fmt[3], fmt[4], rhs.cuda(), 32,
+                                          dimN, 30)[0]
+        ref = _ref(ROW, COL, np.ones(COL.shape[0]), rhs.double().numpy(), 30, 8)
+        assert Y.shape == (30, dimN) and Y.dtype == torch.float32
+        assert np.array_equal(Y.cpu().double().numpy(), ref)
+
+
+def test_reference_balance_test_exact_tf32(cuda):
+    from att_gb300.compat import Block_sr_bcrs, SpMM_sr_bcrs
+    fmt = Block_sr_bcrs.blockProcess_tf32_balance(torch.from_numpy(ROW), torch.from_numpy(COL),
+                                                  torch.ones(32, dtype=torch.float32), 8, 4, 2)
+    rhs = torch.randint(1, 3, (30, 64)).float()
+    fmt = [t.cuda() for t in fmt]
+    Y = SpMM_sr_bcrs.forward_tf32_gnn(fmt[0], fmt[1], fmt[2], fmt[3], fmt[4], rhs.cuda(), 32, 64,
+                                      30)[0]
+    ref = _ref(ROW, COL, np.ones(COL.shape[0]), rhs.double().numpy(), 30, 8)
+    assert np.array_equal(Y.cpu().double().numpy(), ref)
+
+
+@pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16, torch.float32])
+@pytest.mark.parametrize("W,w,P", [(8, 8, 32), (16, 8, 32), (8, 8, 2), (16, 16, 3), (8, 4, 32),
+                                   (16, 4, 5)])
+@pytest.mark.parametrize("F", [32, 64, 128, 256, 96])
+def test_random_power_law_vs_fp64(cuda, dtype, W, w, P, F):
+    from att_gb300 import graphs, ops
+    if (dtype == torch.float32) != (w == 4):
+        if not (dtype == torch.float32 and w == 8):
+            pytest.skip("wide 4 is the fp32 layout")
+    rp_t, col_t = graphs.chung_lu(3000, 12, 2.1, seed=11)
+    rowptr = graphs.pad_rows(rp_t, 8).numpy()
+    col = col_t.numpy()
+    n = 3000
+    deg32 = graphs.gcn_degree(torch.from_numpy(rowptr), torch.float32).numpy()
+    deg32[~np.isfinite(deg32)] = 0
+    deg = deg32.astype(np.float16) if dtype != torch.float32 else deg32
+    f = _format(rowptr, col, deg, W, w, P, emit=(dtype == torch.float32))
+    val = f.val if dtype != torch.bfloat16 else f.val.to(torch.bfloat16)
+    rng = np.random.default_rng(F)
+    X = torch.from_numpy(rng.uniform(-1, 1, size=(n, F)).astype(np.float32)).to(dtype)
+    Y = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, X.cuda(), n, window=W, wide=w)
+    vals = val.float().cpu().numpy()
+    # reference values: the block format's own (rounded) values, per CSR edge
+    ev = oracle.gcn_values(rowptr, col, deg).astype(np.float64)
+    if dtype == torch.bfloat16:
+        ev = torch.from_numpy(ev).to(torch.bfloat16).double().numpy()
+    ref = _ref(rowptr, col, ev, X.double().numpy(), n, W)
+    err = oracle.rel_err(Y.cpu().numpy(), ref)
+    assert err <= TOL[dtype], (dtype, W, w, P, F, err)
+    # error against the unrounded FP64 problem stays within the same bound
+    ev64 = oracle.gcn_values(rowptr, col, deg32).astype(np.float64)
+    ref64 = _ref(rowptr, col, ev64, X.float().double().numpy(), n, W)
+    assert oracle.rel_err(Y.cpu().numpy(), ref64) <= max(TOL[dtype], 1e-2 if dtype != torch.float32 else 1e-4)
+
+
+def test_hub_window_split_and_uncovered_rows(cuda):
+    from att_gb300 import graphs, ops
+    rowptr, col = graphs.random_csr(203, 4000, 9, seed=3, hub_rows=2, hub_len=3500,
+                                    empty_frac=0.3)
+    deg = np.full(4000, 0.5, np.float16)
+    f = _format(rowptr, col, deg, 8, 8, 4)
+    assert int(f.atomic.sum()) > 0
+    X = torch.randn(4000, 64).half().cuda()
+    m_out = 210  # rows past the last window must come back zero
+    Y = torch.full((m_out, 64), float("nan"), device="cuda")
+    ops.spmm(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, X, m_out, window=8, wide=8, out=Y)
+    ev = oracle.gcn_values(rowptr, col, deg).astype(np.float64)
+    ref = _ref(rowptr, col, ev, X.double().cpu().numpy(), m_out, 8)
+    assert oracle.rel_err(Y.cpu().numpy(), ref) <= 1e-2
+    assert torch.all(Y[200:] == 0)
+
+
+def test_bad_column_sets_error_flag(cuda):
+    from att_gb300 import ops
+    f = _format(ROW, COL, np.ones(32, np.float16), 8, 8, 32)
+    col = f.col.clone()
+    col[3] = 1000
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    X = torch.ones(30, 64, dtype=torch.float16, device="cuda")
+    ops.spmm(f.rowptr, col, f.val, f.window_of_part, f.atomic, X, 30, err_flag=err)
+    torch.cuda.synchronize()
+    assert int(err.item()) != 0
