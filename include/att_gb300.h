@@ -113,6 +113,36 @@ ATT_API int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t n_
                    int32_t *out_map, int32_t *out_map_t, int32_t *out_edge_slot,
                    int32_t *out_window, int32_t *out_atomic, void *stream);
 
+/* ----------------------------------------------------------------------
+ * Allocation-free conversion.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory -- hosts that hand out
+ * device memory only from their own arena or budget and forbid a library
+ * from allocating, and latency-critical callers that cannot afford
+ * cudaMalloc/cudaFree, which may synchronise the device.  It does what
+ * att_block_plan + att_block_fill do, in one call, with the scratch taken
+ * from a 64 MiB device array the library owns (att_block_convert_noalloc_max_scratch()
+ * bytes) instead of a caller workspace; it calls no allocating routine.
+ *   - Graphs whose att_block_workspace_bytes() exceeds that size are
+ *     rejected with ATT_ERR_WORKSPACE.
+ *   - Outputs are the caller's, as for att_block_fill; max_parts and
+ *     max_condensed are their capacities (in parts and condensed columns).
+ *     The sizes are written to n_parts_out / n_condensed_out; if they exceed
+ *     the capacities the call returns ATT_ERR_WORKSPACE before writing.
+ *   - The first call on a device looks up the array's device address; make
+ *     it before any stream capture starts.
+ *   - All calls share the array: calls whose GPU work overlaps race.
+ *   - Synchronises `stream` (to read the sizes), like att_block_plan.
+ * ---------------------------------------------------------------------- */
+ATT_API size_t att_block_convert_noalloc_max_scratch(void);
+ATT_API int att_block_convert_noalloc(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
+                   int64_t nnz, int64_t n_cols, int window, int wide, int part, int emit_empty,
+                   const void *deg, int deg_dtype,
+                   int32_t *out_rowptr, int32_t *out_col, void *out_val, int val_dtype,
+                   int32_t *out_map, int32_t *out_map_t, int32_t *out_edge_slot,
+                   int32_t *out_window, int32_t *out_atomic,
+                   int64_t max_parts, int64_t max_condensed,
+                   int64_t *n_parts_out, int64_t *n_condensed_out, void *stream);
+
 /* ======================================================================
  * Blocked SpMM:  Y[m_out, F] = A_blocks * X   (tensor cores, fp32 accumulate)
  * Replaces SpMM_sr_bcrs.forward_fp16_gnn / forward_tf32_gnn /
