@@ -257,7 +257,7 @@ def run_reference(args):
     import torch
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     t_setup = time.time()
-    wl = WORKLOADS[args.workload](dev)
+    wl = WORKLOADS[args.workload](dev, scale=args.scale)
     base = cpu_baseline(wl, budget_s=max(3.0, 20.0 / max(1, args.steps + args.warmup)))
     line = {"metric": METRIC, "impl": "reference", "value": base["value"], "unit": wl.unit,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -281,6 +281,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="node-count scale of the workload (1.0 = the named config)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -300,7 +302,7 @@ def main():
     from att_gb300 import _lib
     _lib.load()
 
-    wl = WORKLOADS[args.workload]("cuda")
+    wl = WORKLOADS[args.workload]("cuda", scale=args.scale)
     check_err = wl.check()
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
