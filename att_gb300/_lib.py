@@ -39,6 +39,18 @@ _SIGNATURES = {
     "att_spmm": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_i64, _c_vp, _c_int,
                           _c_vp, _c_i64, _c_i64, _c_i64, _c_vp, _c_i64, _c_i64, _c_int, _c_int,
                           _c_vp, _c_vp]),
+    "att_node_scores": (_c_int, [_c_vp, _c_int, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64, _c_vp,
+                                 _c_int, _c_i64, _c_vp, _c_i64, _c_vp]),
+    "att_slot_edges": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_int,
+                                _c_vp, _c_vp, _c_i64, _c_vp, _c_int, _c_i64, _c_i64, _c_i64,
+                                _c_i64, _c_vp, _c_int, _c_i64, _c_i64, _c_vp]),
+    "att_sddmm": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_vp, _c_vp,
+                           _c_int, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64,
+                           _c_i64, _c_vp, _c_int, _c_i64, _c_i64, _c_vp, _c_vp]),
+    "att_gather_slot_values": (_c_int, [_c_vp, _c_i64, _c_int, _c_int, _c_int, _c_vp, _c_int,
+                                        _c_i64, _c_i64, _c_i64, _c_vp, _c_int, _c_i64, _c_vp]),
+    "att_rowsum": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_vp, _c_int,
+                            _c_i64, _c_i64, _c_i64, _c_vp, _c_i64, _c_i64, _c_i64, _c_vp]),
 }
 
 _lib = None

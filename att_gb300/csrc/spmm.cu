@@ -40,11 +40,21 @@ struct PartInfo {
     int start, nreal, nsteps;
 };
 
-__device__ __forceinline__ PartInfo part_info(const int32_t *__restrict__ rowptr, int64_t p) {
+// A part must start and end on a block boundary of the layout the kernel
+// reads (the value tile of a 16-column step is read whole); a part that does
+// not is flagged and skipped instead of read past its end.
+template <int WIDE>
+__device__ __forceinline__ PartInfo part_info(const int32_t *__restrict__ rowptr, int64_t p,
+                                              int32_t *err) {
     PartInfo pi;
     pi.start = __ldg(rowptr + 2 * p);
-    int e = __ldg(rowptr + 2 * p + 1);
+    const int e = __ldg(rowptr + 2 * p + 1);
+    const int pend = __ldg(rowptr + 2 * p + 2);
     pi.nreal = e > pi.start ? e - pi.start : 0;
+    if ((pi.start % WIDE) != 0 || (pend % WIDE) != 0 || pend < pi.start + pi.nreal) {
+        if (err) atomicOr(err, 2);
+        pi.nreal = 0;
+    }
     pi.nsteps = (pi.nreal + 15) >> 4;
     return pi;
 }
@@ -98,7 +108,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
         while (p_item < n_items) {
             int64_t part = p_item / n_chunks;
             p_fc = (int)(p_item - part * n_chunks);
-            p_pi = part_info(rowptr, part);
+            p_pi = part_info<WIDE>(rowptr, part, err);
             p_step = 0;
             if (p_pi.nsteps > 0) return;
             p_item += stride;
@@ -162,7 +172,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
     for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
         const int64_t part = c_item / n_chunks;
         const int fc = (int)(c_item - part * n_chunks);
-        const PartInfo pi = part_info(rowptr, part);
+        const PartInfo pi = part_info<WIDE>(rowptr, part, err);
         for (int step = 0; step < pi.nsteps; ++step) {
             cp_async_wait<kStages - 2>();
             __syncwarp();
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
         while (p_item < n_items) {
             int64_t part = p_item / n_chunks;
             p_fc = (int)(p_item - part * n_chunks);
-            p_pi = part_info(rowptr, part);
+            p_pi = part_info<WIDE>(rowptr, part, err);
             p_step = 0;
             if (p_pi.nsteps > 0) return;
             p_item += stride;
@@ -338,7 +348,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
     for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
         const int64_t part = c_item / n_chunks;
         const int fc = (int)(c_item - part * n_chunks);
-        const PartInfo pi = part_info(rowptr, part);
+        const PartInfo pi = part_info<WIDE>(rowptr, part, err);
         for (int step = 0; step < pi.nsteps; ++step) {
             cp_async_wait<kStages - 2>();
             __syncwarp();

@@ -159,14 +159,82 @@ ATT_API int att_block_convert_noalloc(const int32_t *rowptr, const int32_t *col,
  *   Every row of Y in [0, m_out) is written (rows of windows without parts
  *   are zeroed), so Y needs no prior clearing.
  *   window: 8 or 16; wide: 8 or 16 for 16-bit values, 4 or 8 for fp32.
- *   err_flag (device int32, may be NULL): set non-zero if a column id is
- *   outside [-1, n_x_rows); such columns contribute nothing.
+ *   err_flag (device int32, may be NULL): bit 1 set if a column id is
+ *   outside [-1, n_x_rows) (such columns contribute nothing); bit 2 set if a
+ *   part does not start and end on a `wide` block boundary (it is skipped).
  * ====================================================================== */
 ATT_API int att_spmm(const int32_t *rowptr, const int32_t *col, const void *val, int val_dtype,
              const int32_t *window_of_part, const int32_t *atomic, int64_t n_parts,
              const void *X, int x_dtype, const float *x_scale, int64_t n_x_rows,
              int64_t F, int64_t ldx, float *Y, int64_t m_out, int64_t ldy,
              int window, int wide, int32_t *err_flag, void *stream);
+
+/* ======================================================================
+ * GAT operators on the block format with a slot -> edge map (the format
+ * att_block_fill writes with `map` / `map_t`).  They replace the
+ * ATT_SDDMM_v{1,3,4} and ATT_SpMM_v{1,3,4} extension ops, whose CUDA source
+ * is absent from the reference; the meaning of each is pinned by the
+ * reference's tests (benchmark-v3/sddmm-benchmark/test/*,
+ * benchmark-v3/spmm-benchmark/test/*) and callers
+ * (end2end_ori/gat_final/mgat_csr/mgat_conv.py:14-198,
+ * end2end_head/gat_final/mgat_csr/mgat_conv.py:14-198,
+ * end2end_acc/gat_final/mgat_csr/mgat_conv.py:16-232).
+ * Edge-valued arrays are addressed base[h*stride_h + e*stride_e] and
+ * node-valued arrays base[h*stride_h + node*stride_n], so [h,nnz] / [nnz,h]
+ * and [h,M,F] / [M,h,F] layouts are views.  Edge ids are CSR positions.
+ * ====================================================================== */
+
+/* scores[h][m] = sum_f X[h][m][f] * a[h][f]  (fp32 accumulate).  Building
+ * block of att_*_h_nnz / attv2_*_h_nnz (mgat_conv.py:21-30). */
+ATT_API int att_node_scores(const void *X, int x_dtype, int64_t n_heads, int64_t n_nodes,
+                   int64_t F, int64_t x_stride_h, int64_t x_stride_n, const void *a,
+                   int a_dtype, int64_t a_stride_h, float *scores, int64_t s_stride_h,
+                   void *stream);
+
+/* For every slot with an edge e (row i = window*W + r, column j = col[c]):
+ *   mode 0: out[h][e] = s0[h][i] + s1[h][j]   (att_*_h_nnz: X_i.a0 + X_j.a1;
+ *           attv2_*_h_nnz: X0_i.a + X1_j.a; test_sddmm_tf32_att.py,
+ *           test_sddmm_fp16_att_v2.py:70-77)
+ *   mode 1: out[h][e] = g[h][i]               (sddmm_*_ones_h_nnz,
+ *           test_sddmm_fp16_ones.py:62-68)
+ * Edges no slot holds are not written. */
+ATT_API int att_slot_edges(const int32_t *rowptr, const int32_t *col, const int32_t *map,
+                   const int32_t *window_of_part, int64_t n_parts, int window, int wide,
+                   int mode, const float *s0, const float *s1, int64_t s_stride_h,
+                   const void *g, int g_dtype, int64_t g_stride_h, int64_t g_stride_n,
+                   int64_t n_nodes, int64_t n_heads, void *out, int out_dtype,
+                   int64_t out_stride_h, int64_t out_stride_e, void *stream);
+
+/* Blocked SDDMM: out[h][e(i,j)] = A[h][i] . B[h][j] for every slot with an edge
+ * (sddmm_*_h_nnz, test_sddmm_fp16.py:62-69; mgat_conv.py:109-117).  Tensor
+ * cores: mma.sync m16n8k16 (dtype ATT_F16 / ATT_BF16, fp32 accumulate) or a
+ * 3xTF32 m16n8k8 split (ATT_F32).  F <= 256 (<= 128 for fp32); wide 4/8/16;
+ * 16-bit B rows need F and strides multiples of 8 (16-byte rows). */
+ATT_API int att_sddmm(const int32_t *rowptr, const int32_t *col, const int32_t *map,
+                   const int32_t *window_of_part, int64_t n_parts, int window, int wide,
+                   const void *A, const void *B, int dtype, int64_t n_heads, int64_t F,
+                   int64_t a_stride_h, int64_t a_stride_n, int64_t n_a,
+                   int64_t b_stride_h, int64_t b_stride_n, int64_t n_b, void *out,
+                   int out_dtype, int64_t out_stride_h, int64_t out_stride_e,
+                   int32_t *err_flag, void *stream);
+
+/* Dense block values from per-edge values: out[h][s] = vals[h][map[s']] or 0,
+ * where s (block width out_wide) and s' (block width map_wide) name the same
+ * (window row, condensed column).  With att_spmm this is spmm_*_h_m / _m_h
+ * (test_spmm_h_m.py:45-66, test_spmm_m_h.py:47-80; mgat_conv.py:79-86,99-106). */
+ATT_API int att_gather_slot_values(const int32_t *map, int64_t n_slots, int window,
+                   int map_wide, int out_wide, const void *vals, int v_dtype,
+                   int64_t v_stride_h, int64_t v_stride_e, int64_t n_heads,
+                   void *out, int out_dtype, int64_t out_stride_h, void *stream);
+
+/* Row sums of per-edge values through the map: out[h][i] = sum over slots of
+ * row i of vals[h][map[s]] (spmm_*_{h_m,m_h}_rowsum, test_spmm_h_m_ones.py:45-68;
+ * mgat_conv.py:126-132).  Every row < m_out is written (fp32). */
+ATT_API int att_rowsum(const int32_t *rowptr, const int32_t *map,
+                   const int32_t *window_of_part, const int32_t *atomic, int64_t n_parts,
+                   int window, int wide, const void *vals, int v_dtype, int64_t v_stride_h,
+                   int64_t v_stride_e, int64_t n_heads, float *out, int64_t out_stride_h,
+                   int64_t out_stride_n, int64_t m_out, void *stream);
 
 #ifdef __cplusplus
 }
