@@ -27,7 +27,12 @@
 //    windows, windows without parts, trailing rows), so Y needs no memset.
 #include "att_common.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <mutex>
+#include <string.h>
+#include <type_traits>
 
 namespace att {
 namespace {
@@ -237,6 +242,225 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
         }
     }
     cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// 16-bit operand kernel fed by TMA: tile::gather4 row gathers
+// ---------------------------------------------------------------------------
+// Same contraction and epilogue as k_spmm16; the producer is one bulk-tensor
+// instruction per 4 gathered rows and 64 features instead of 16 cp.async per
+// lane.  X is described by a 2-D tensor map (features x rows) with an
+// 80 x 1 box and no swizzle: a gathered row occupies 160 bytes, so the 8 rows
+// an ldmatrix reads fall on distinct 32-byte bank groups within a 4-row group
+// (two groups share them: 2-way), and 4 rows (640 bytes) keep every TMA
+// destination 128-byte aligned without padding.  Of the 80 features, the 64
+// wanted plus 16 chosen outside [0, F) where possible (left of feature 0, or
+// right of the last), which TMA zero-fills without reading memory.  Rows of
+// padding columns are fetched from row n_x, outside the tensor, also
+// zero-filled.  The step's value tile is one contiguous bulk copy.  Each
+// stage completes on an mbarrier carrying the byte count; every wait is
+// bounded, and a timeout raises bit 4 of err and ends the warp after draining
+// its copies in flight.
+constexpr uint32_t kMaxPolls = 1u << 24;
+constexpr int kBox = 80;            // features per TMA box
+constexpr int kPitch = kBox * 2;    // bytes per gathered row in shared memory
+constexpr int kGroup = 4 * kPitch;  // one gather4 destination (640 B, 128-aligned)
+
+template <int W, int FC, int S>
+struct CfgTma {
+    static constexpr int FCH = FC / 64;            // 64-feature boxes per gathered row
+    static constexpr int CHUNK = 4 * kGroup;       // 16 rows of one box
+    static constexpr int XSTAGE = FCH * CHUNK;
+    static constexpr int VSTAGE = 16 * W * 2;
+    static constexpr int STAGE = (XSTAGE + VSTAGE + 127) / 128 * 128;
+    static constexpr int WARP_SMEM = (S * STAGE + S * 8 + 127) / 128 * 128;
+    static constexpr int SMEM = kWarps * WARP_SMEM + 128;  // + alignment slack
+    static constexpr int MT = FC / 16;
+    static constexpr int NT = W / 8;
+};
+
+// 16 of the 80 features of a box are extra: to the left of `fb` (box starts
+// at fb - 16) unless the right side is past F (box starts at fb)
+__device__ __forceinline__ bool box_left(int64_t fb, int64_t F) { return fb == 0 || fb + 64 < F; }
+
+template <typename T, int W, int FC, int WIDE, int S>
+__global__ void __launch_bounds__(kThreads) k_spmm16_tma(
+    const __grid_constant__ CUtensorMap tmX, const int32_t *__restrict__ rowptr,
+    const int32_t *__restrict__ col, const T *__restrict__ val, const int32_t *__restrict__ win,
+    const int32_t *__restrict__ atomic, int64_t n_parts, int64_t n_x, int64_t F,
+    float *__restrict__ Y, int64_t m_out, int64_t ldy, int n_chunks, int32_t *__restrict__ err) {
+    using C = CfgTma<W, FC, S>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = ((smem_u32(smem) + 127u) & ~127u) + warp * C::WARP_SMEM;
+    const int64_t n_items = n_parts * n_chunks;
+    const int64_t stride = (int64_t)gridDim.x * kWarps;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int oob_row = (int)n_x;  // one past the last row: zero-filled by TMA
+    auto xstage = [&](int stage) { return sbase + stage * C::STAGE; };
+    auto vtile = [&](int stage) { return sbase + stage * C::STAGE + C::XSTAGE; };
+    auto sbar = [&](int stage) { return sbase + S * C::STAGE + 8 * stage; };
+
+    // value tiles start zeroed (a tile whose second block lies past its part
+    // keeps finite data that only ever meets zero rows); barriers armed once
+    for (int st = 0; st < S; ++st)
+        for (int i = lane; i < C::VSTAGE / 4; i += 32)
+            asm volatile("st.shared.u32 [%0], %1;\n" ::"r"(vtile(st) + 4 * i), "r"(0) : "memory");
+    if (lane == 0) {
+        for (int st = 0; st < S; ++st) mbar_init(sbar(st), 1);
+        mbar_fence_init();
+    }
+    fence_proxy_async_smem();
+    __syncwarp();
+
+    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    int p_step = 0, p_fc = 0, p_pend = 0;
+    PartInfo p_pi = {0, 0, 0};
+    auto p_load = [&]() {
+        while (p_item < n_items) {
+            int64_t part = p_item / n_chunks;
+            p_fc = (int)(p_item - part * n_chunks);
+            p_pi = part_info<WIDE>(rowptr, part, err);
+            p_pend = __ldg(rowptr + 2 * part + 2);
+            p_step = 0;
+            if (p_pi.nsteps > 0) return;
+            p_item += stride;
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t bar = sbar(stage);
+        const int c0 = p_step * 16;
+        const int vcols = min(16, p_pend - p_pi.start - c0);
+        const uint32_t vbytes = (uint32_t)(vcols * W * 2);
+        if (lane == 0) mbar_arrive_expect_tx(bar, C::FCH * 4 * 4 * kPitch + vbytes);
+        __syncwarp();
+        if (lane < 4) {
+            int y[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int c = c0 + 4 * lane + i;
+                int cidx = c < p_pi.nreal ? __ldg(col + p_pi.start + c) : -1;
+                if (cidx >= n_x || cidx < -1) {
+                    if (err) atomicOr(err, 1);
+                    cidx = -1;
+                }
+                y[i] = cidx >= 0 ? cidx : oob_row;
+            }
+#pragma unroll
+            for (int ch = 0; ch < C::FCH; ++ch) {
+                const int64_t fb = (int64_t)p_fc * FC + 64 * ch;
+                const int x = (int)(box_left(fb, F) ? fb - 16 : fb);
+                tma_gather4(xstage(stage) + ch * C::CHUNK + lane * kGroup, &tmX, x, y[0], y[1], y[2],
+                            y[3], bar);
+            }
+        } else if (lane == 4) {
+            bulk_g2s(vtile(stage), val + (int64_t)(p_pi.start + c0) * W, vbytes, bar);
+        }
+    };
+    auto p_advance = [&]() {
+        if (++p_step >= p_pi.nsteps) {
+            p_item += stride;
+            p_load();
+        }
+    };
+
+    p_load();
+    int inflight = 0;
+#pragma unroll
+    for (int s = 0; s < S - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+            ++inflight;
+        }
+    }
+
+    float acc[C::MT][C::NT][4];
+#pragma unroll
+    for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
+
+    uint32_t phase = 0;  // bit s: parity of stage s's next completion
+    int cstage = 0, pstage = S - 1;
+    for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const int64_t part = c_item / n_chunks;
+        const int fc = (int)(c_item - part * n_chunks);
+        const PartInfo pi = part_info<WIDE>(rowptr, part, nullptr);
+        for (int step = 0; step < pi.nsteps; ++step) {
+            const uint32_t bar = sbar(cstage);
+            if (!mbar_wait_bounded(bar, (phase >> cstage) & 1u, kMaxPolls)) {
+                // give up: record it, drain the copies still in flight, leave
+                if (lane == 0 && err) atomicOr(err, 4);
+                for (int k = 1; k < inflight; ++k) {
+                    const int s2 = (cstage + k) % S;
+                    mbar_wait_bounded(sbar(s2), (phase >> s2) & 1u, kMaxPolls);
+                }
+                return;
+            }
+            phase ^= 1u << cstage;
+            --inflight;
+            const uint32_t vs = vtile(cstage);
+            uint32_t b[C::NT][2];
+            {
+                const int q = lane >> 3, rr = lane & 7;
+                if constexpr (C::NT == 2) {
+                    const int kb = q & 1, r = (q >> 1) * 8 + rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x4(vs + e * 2, b[0][0], b[0][1], b[1][0], b[1][1]);
+                } else {
+                    const int kb = q & 1, r = rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x2(vs + e * 2, b[0][0], b[0][1]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int q = lane >> 3, rr = lane & 7;
+                const int k = (q >> 1) * 8 + rr;
+                const int bx = j >> 2;  // 64-feature box
+                const int fo = (box_left((int64_t)fc * FC + 64 * bx, F) ? 16 : 0) + (j & 3) * 16 +
+                               (q & 1) * 8;
+                uint32_t a[4];
+                ldsm_x4_trans(xstage(cstage) + bx * C::CHUNK + (k >> 2) * kGroup + (k & 3) * kPitch +
+                                  fo * 2,
+                              a[0], a[1], a[2], a[3]);
+#pragma unroll
+                for (int t = 0; t < C::NT; ++t) mma_16816<T>(acc[j][t], a, b[t][0], b[t][1]);
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                fence_proxy_async_smem();
+                issue(pstage);
+                p_advance();
+                ++inflight;
+            }
+            cstage = cstage + 1 == S ? 0 : cstage + 1;
+            pstage = pstage + 1 == S ? 0 : pstage + 1;
+        }
+        const int wrow = __ldg(win + part);
+        const bool add = __ldg(atomic + part) != 0;
+        const int64_t f0 = (int64_t)fc * FC;
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) {
+            const int64_t r0 = (int64_t)wrow * W + t * 8 + 2 * tig;
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int64_t fa = f0 + 16 * j + gid;
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int64_t r = r0 + (h & 1);
+                    const int64_t f = fa + (h >> 1) * 8;
+                    if (r >= 0 && r < m_out && f < F) {
+                        float *dst = Y + r * ldy + f;
+                        if (add) red_add_f32(dst, acc[j][t][h]);
+                        else *dst = acc[j][t][h];
+                    }
+                    acc[j][t][h] = 0.f;
+                }
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -499,11 +723,73 @@ int launch_tf32(const int32_t *rowptr, const int32_t *col, const void *val, cons
     return launch_status("k_spmm_tf32");
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+template <typename T, int W, int FC, int WIDE, int S>
+int launch16_tma(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+                 const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
+                 int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err, cudaStream_t st) {
+    using C = CfgTma<W, FC, S>;
+    auto kernel = k_spmm16_tma<T, W, FC, WIDE, S>;
+    static std::once_flag once;
+    static int prep = ATT_OK;
+    std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+    if (prep != ATT_OK) return prep;
+    const int n_chunks = (int)((F + FC - 1) / FC);
+    const int64_t items = n_parts * n_chunks;
+    if (items == 0) return ATT_OK;
+    CUtensorMap tm;
+    const cuuint64_t gdim[2] = {(cuuint64_t)F, (cuuint64_t)n_x};
+    const cuuint64_t gstride[1] = {(cuuint64_t)ldx * sizeof(T)};
+    const cuuint32_t box[2] = {(cuuint32_t)kBox, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = tensor_map_encoder()(
+        &tm, sizeof(T) == 2 && std::is_same<T, __half>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                               : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+        2, const_cast<void *>(X), gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    ATT_CHECK(r == CUDA_SUCCESS, ATT_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    const int grid = occupancy_grid(kernel, C::SMEM, items);
+    kernel<<<grid, kThreads, C::SMEM, st>>>(tm, rowptr, col, (const T *)val, win, atomic, n_parts,
+                                            n_x, F, Y, m_out, ldy, n_chunks, err);
+    return launch_status("k_spmm16_tma");
+}
+
+constexpr int kTmaStages = 5;
+
+// Row-gather mechanism of the 16-bit kernel: 0 = cp.async (default, measured
+// faster on the 2.45M-node graph), 1 = TMA tile::gather4.  Set through
+// att_set_option("spmm_gather", ...).
+int g_spmm_gather = 0;
+
 template <typename T, int W, int WIDE>
 int dispatch_fc16(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
                   const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
                   int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err,
                   cudaStream_t st) {
+    // TMA row gathers for F >= 64 (the tensor map's 64-feature box fits); the
+    // cp.async kernel for narrower features or an X without rows
+    if (g_spmm_gather == 1 && F >= 64 && n_x > 0 && n_x < INT32_MAX &&
+        tensor_map_encoder() != nullptr) {
+        if (F <= 64)
+            return launch16_tma<T, W, 64, WIDE, kTmaStages>(rowptr, col, val, win, atomic, n_parts,
+                                                            X, n_x, F, ldx, Y, m_out, ldy, err, st);
+        return launch16_tma<T, W, 128, WIDE, kTmaStages>(rowptr, col, val, win, atomic, n_parts, X,
+                                                         n_x, F, ldx, Y, m_out, ldy, err, st);
+    }
     if (F <= 32)
         return launch16<T, W, 32, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
                                         m_out, ldy, err, st);
@@ -603,4 +889,27 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
     (void)x_scale;
     set_error("unsupported (val_dtype=%d, x_dtype=%d) combination", val_dtype, x_dtype);
     return ATT_ERR_UNSUPPORTED;
+}
+
+extern "C" int att_set_option(const char *key, int value) {
+    clear_error();
+    ATT_CHECK(key != nullptr, ATT_ERR_INVALID, "null option name");
+    if (strcmp(key, "spmm_gather") == 0) {
+        ATT_CHECK(value == 0 || value == 1, ATT_ERR_INVALID, "spmm_gather must be 0 or 1");
+        g_spmm_gather = value;
+        return ATT_OK;
+    }
+    set_error("unknown option '%s'", key);
+    return ATT_ERR_INVALID;
+}
+
+extern "C" int att_get_option(const char *key, int *value) {
+    clear_error();
+    ATT_CHECK(key != nullptr && value != nullptr, ATT_ERR_INVALID, "null argument");
+    if (strcmp(key, "spmm_gather") == 0) {
+        *value = g_spmm_gather;
+        return ATT_OK;
+    }
+    set_error("unknown option '%s'", key);
+    return ATT_ERR_INVALID;
 }

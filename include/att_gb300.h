@@ -60,6 +60,12 @@ enum att_dtype {
     ATT_NONE = -1
 };
 
+/* Process-wide tuning knobs (no counterpart in the reference).
+ *   "spmm_gather": 0 = 16-byte cp.async row gathers (default),
+ *                  1 = TMA tile::gather4 row gathers (F >= 64). */
+ATT_API int att_set_option(const char *key, int value);
+ATT_API int att_get_option(const char *key, int *value);
+
 /* Human-readable name of a status. */
 ATT_API const char *att_status_string(int status);
 /* Message of the last failing call on this host thread ("" if none). */
