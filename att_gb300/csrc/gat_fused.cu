@@ -1,0 +1,570 @@
+// gat_fused.cu -- one-pass GAT attention layer on the row-window block format.
+//
+// Replaces the reference's chain of separate ops for a GAT layer
+// (end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198: att/SDDMM ->
+// LeakyReLU -> exp -> row sums -> SpMM -> divide, each a kernel with an
+// nnz-sized intermediate) by one kernel that never materialises per-edge
+// values.  Per 8-row window and 16 condensed columns at a time:
+//
+//   logits  mode 0 (dot):      S[c][r] = X'_c . X'_r  -- mma.sync m16n8k16, K = F
+//           mode 1 (additive): S[c][r] = s0[r] + s1[c] -- GAT's a0/a1 scores
+//   e = LeakyReLU(S) on occupied slots (per-slot bitmap), -inf elsewhere
+//   online softmax: running row max m and sum l in fp32 registers, reduced
+//     across the 8 lanes of a row with shuffles; the accumulator is rescaled
+//     by exp(m_old - m_new) whenever the max grows
+//   P = exp(e - m) -> fp16/bf16, transposed in registers (movmatrix) into the
+//     B operand of acc[f][r] += X'^T[f][c] . P[c][r]  -- mma.sync m16n8k16
+//
+// X' rows of the 16 columns are gathered once per step (16-byte cp.async into
+// a 4-stage per-warp ring, XOR-swizzled) and feed both products.
+// A work item is a chunk of up to `parts_per_chunk` consecutive parts of one
+// window; a window covered by one chunk is finalised in place (out = acc/l,
+// plus the row max and sum for the backward pass); a window spread over
+// several chunks writes (m, l, acc) partials that k_gat_combine merges.
+#include "att_common.cuh"
+
+#include <mutex>
+
+namespace att {
+namespace {
+
+constexpr int kGWarps = 4;
+constexpr int kGThreads = kGWarps * 32;
+constexpr int kGStages = 4;
+constexpr int kW = 8;  // window rows
+
+__device__ __forceinline__ uint32_t movmatrix_trans(uint32_t x) {
+    uint32_t y;
+    asm volatile("movmatrix.sync.aligned.m8n8.trans.b16 %0, %1;\n" : "=r"(y) : "r"(x));
+    return y;
+}
+
+template <typename T>
+__device__ __forceinline__ uint32_t pack2(float lo, float hi);
+template <>
+__device__ __forceinline__ uint32_t pack2<__half>(float lo, float hi) {
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+template <>
+__device__ __forceinline__ uint32_t pack2<__nv_bfloat16>(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
+                 "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src),
+                 "r"(src_bytes));
+}
+
+struct GatArgs {
+    const int32_t *rowptr, *col, *win;
+    const uint32_t *mask;         // occupancy bit per slot
+    const int32_t *chunk_begin;   // [n_chunks + 1] part ranges
+    const int32_t *chunk_slot;    // [n_chunks] partial slot or -1 (whole window)
+    int64_t n_chunks;
+    int wide;
+    const void *X;                // X' rows: X + node * ldx + head * F
+    int64_t n_nodes, H, F, ldx;
+    int mode;
+    const float *s0, *s1;         // [H][n_nodes] node scores (mode 1)
+    float slope;
+    float *out;                   // [n_nodes, H*F] rows of ldo
+    int64_t ldo;
+    float *row_max, *row_sum;     // [H][n_nodes] or null
+    float *partial;               // [n_partial][H][kW][F + 2]
+    int32_t *err;
+};
+
+template <int F>
+__device__ __forceinline__ int swz_row(int r) {
+    if constexpr (F * 2 >= 128) return r & 7;
+    else return (r >> 1) & 3;
+}
+
+template <typename T, int F, int MODE>
+struct GCfg {
+    static constexpr int XROW = F * 2;
+    static constexpr int XSTAGE = 16 * XROW;
+    static constexpr int MSTAGE = 16;            // 128 occupancy bits
+    static constexpr int SSTAGE = MODE == 1 ? 64 : 0;  // s1 of the 16 columns
+    static constexpr int STAGE = XSTAGE + MSTAGE + SSTAGE;
+    static constexpr int WARP_SMEM = kGStages * STAGE;
+    static constexpr int SMEM = kGWarps * WARP_SMEM;
+    static constexpr int CPR = XROW / 16;
+    static constexpr int PASSES = (16 * CPR + 31) / 32;
+    static constexpr int MT = F / 16;
+};
+
+template <typename T, int F, int MODE>
+__global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
+    using C = GCfg<T, F, MODE>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
+    const unsigned char *sgen = smem + warp * C::WARP_SMEM;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int64_t n_items = A.n_chunks * A.H;
+    const int64_t stride = (int64_t)gridDim.x * kGWarps;
+    const T *X = (const T *)A.X;
+    const float NEG_INF = -INFINITY;
+
+    // ---- producer: (item, part, step) cursor ----
+    int64_t p_item = (int64_t)blockIdx.x * kGWarps + warp;
+    int64_t p_h = 0;
+    int p_part = 0, p_part_end = 0, p_start = 0, p_nreal = 0, p_pend = 0, p_step = 0;
+    auto p_set_part = [&]() {  // returns with p_part < p_part_end and a non-empty part, or exhausted
+        while (true) {
+            while (p_part < p_part_end) {
+                p_start = A.rowptr[2 * p_part];
+                const int e = A.rowptr[2 * p_part + 1];
+                p_pend = A.rowptr[2 * p_part + 2];
+                p_nreal = e > p_start ? e - p_start : 0;
+                if ((p_start % A.wide) != 0 || (p_pend % A.wide) != 0 || p_pend < p_start + p_nreal) {
+                    if (A.err) atomicOr(A.err, 2);
+                    p_nreal = 0;
+                }
+                p_step = 0;
+                if (p_nreal > 0) return;
+                ++p_part;
+            }
+            p_item += stride;
+            if (p_item >= n_items) return;
+            const int64_t ch = p_item / A.H;
+            p_h = p_item - ch * A.H;
+            p_part = A.chunk_begin[ch];
+            p_part_end = A.chunk_begin[ch + 1];
+        }
+    };
+    auto p_begin = [&]() {
+        if (p_item < n_items) {
+            const int64_t ch = p_item / A.H;
+            p_h = p_item - ch * A.H;
+            p_part = A.chunk_begin[ch];
+            p_part_end = A.chunk_begin[ch + 1];
+            p_set_part();
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * C::STAGE;
+        const uint32_t ms = xs + C::XSTAGE;
+        const uint32_t ss = ms + C::MSTAGE;
+        const int c0 = p_step * 16;
+        int myc = -1;
+        if (c0 + (lane & 15) < p_nreal) myc = A.col[p_start + c0 + (lane & 15)];
+        if (myc >= A.n_nodes || myc < -1) {
+            if (A.err) atomicOr(A.err, 1);
+            myc = -1;
+        }
+#pragma unroll
+        for (int i = 0; i < C::PASSES; ++i) {
+            const int idx = i * 32 + lane;
+            const int r = idx / C::CPR, ch = idx % C::CPR;
+            const int cidx = __shfl_sync(0xffffffffu, myc, r & 15);
+            if (idx < 16 * C::CPR) {
+                const bool ok = cidx >= 0;
+                const T *src = ok ? X + (int64_t)cidx * A.ldx + p_h * F + ch * 8 : X;
+                cp_async16(xs + r * C::XROW + ((ch ^ swz_row<F>(r)) << 4), src, ok ? 16 : 0);
+            }
+        }
+        // occupancy bits of the step's 16 x 8 slots, one 8-byte piece per
+        // 8-column half (a half past the part's padded end is zero-filled)
+        if (lane < 2) {
+            const bool ok = c0 + 8 * lane < p_pend - p_start;
+            const int64_t bit0 = (int64_t)(p_start + c0 + 8 * lane) * kW;
+            const uint32_t *src = ok ? A.mask + (bit0 >> 5) : A.mask;
+            cp_async8(ms + 8 * lane, src, ok ? 8 : 0);
+        }
+        if constexpr (MODE == 1) {
+            if (lane < 16) {
+                const int c = __shfl_sync(0x0000ffffu, myc, lane);
+                const bool ok = c >= 0;
+                cp_async4(ss + 4 * lane, ok ? (const void *)(A.s1 + p_h * A.n_nodes + c)
+                                            : (const void *)A.s1,
+                          ok ? 4 : 0);
+            }
+        } else {
+            (void)ss;
+        }
+    };
+    auto p_advance = [&]() {
+        if (++p_step * 16 >= p_nreal) {
+            ++p_part;
+            p_set_part();
+        }
+    };
+
+    p_begin();
+#pragma unroll
+    for (int s = 0; s < kGStages - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+        cp_async_commit();
+    }
+
+    int cstage = 0, pstage = kGStages - 1;
+    for (int64_t c_item = (int64_t)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
+        const int64_t chunk = c_item / A.H;
+        const int64_t h = c_item - chunk * A.H;
+        const int part0 = A.chunk_begin[chunk], part1 = A.chunk_begin[chunk + 1];
+        if (part1 <= part0) continue;
+        const int64_t wrow = (int64_t)A.win[part0] * kW;
+        // query side of the window: B fragments (mode 0) or row scores (mode 1)
+        uint32_t bq[C::MT][2];
+        float s0r[2] = {0.f, 0.f};
+        if constexpr (MODE == 0) {
+#pragma unroll
+            for (int kk = 0; kk < C::MT; ++kk)
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int64_t row = wrow + gid;
+                    const int f = 16 * kk + 2 * tig + 8 * u;
+                    bq[kk][u] = row < A.n_nodes
+                                    ? *(const uint32_t *)(X + row * A.ldx + h * F + f)
+                                    : 0u;
+                }
+        } else {
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int64_t row = wrow + 2 * tig + u;
+                s0r[u] = row < A.n_nodes ? A.s0[h * A.n_nodes + row] : 0.f;
+            }
+        }
+        float m_run[2] = {NEG_INF, NEG_INF}, l_run[2] = {0.f, 0.f};
+        float acc[C::MT][4];
+#pragma unroll
+        for (int j = 0; j < C::MT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+
+        for (int part = part0; part < part1; ++part) {
+            const int start = A.rowptr[2 * part];
+            const int e = A.rowptr[2 * part + 1];
+            const int pend = A.rowptr[2 * part + 2];
+            int nreal = e > start ? e - start : 0;
+            if ((start % A.wide) != 0 || (pend % A.wide) != 0 || pend < start + nreal) nreal = 0;
+            const int nsteps = (nreal + 15) >> 4;
+            for (int step = 0; step < nsteps; ++step) {
+                cp_async_wait<kGStages - 2>();
+                __syncwarp();
+                const uint32_t xs = sbase + cstage * C::STAGE;
+                const uint32_t *mw = (const uint32_t *)(sgen + cstage * C::STAGE + C::XSTAGE);
+                // logits S[col][row]: this lane holds cols (gid, gid+8) x rows (2tig, 2tig+1)
+                float sv[4];
+                if constexpr (MODE == 0) {
+                    sv[0] = sv[1] = sv[2] = sv[3] = 0.f;
+#pragma unroll
+                    for (int kk = 0; kk < C::MT; ++kk) {
+                        const int q = lane >> 3, rr = lane & 7;
+                        const int mrow = (q & 1) * 8 + rr;
+                        const int ch = 2 * kk + (q >> 1);
+                        uint32_t a[4];
+                        ldsm_x4(xs + mrow * C::XROW + ((ch ^ swz_row<F>(mrow)) << 4), a[0], a[1],
+                                a[2], a[3]);
+                        mma_16816<T>(sv, a, bq[kk][0], bq[kk][1]);
+                    }
+                } else {
+                    const float *s1s = (const float *)(sgen + cstage * C::STAGE + C::XSTAGE + C::MSTAGE);
+                    const float c_lo = s1s[gid], c_hi = s1s[gid + 8];
+                    sv[0] = s0r[0] + c_lo;
+                    sv[1] = s0r[1] + c_lo;
+                    sv[2] = s0r[0] + c_hi;
+                    sv[3] = s0r[1] + c_hi;
+                }
+                // LeakyReLU on occupied slots, -inf on empty ones
+                const int c0 = step * 16;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int c = gid + 8 * (u >> 1);
+                    const int r = 2 * tig + (u & 1);
+                    const int bit = (c - c % A.wide) * kW + r * A.wide + c % A.wide;
+                    const bool occ = c0 + c < nreal && ((mw[bit >> 5] >> (bit & 31)) & 1u);
+                    const float x = sv[u];
+                    sv[u] = occ ? (x > 0.f ? x : A.slope * x) : NEG_INF;
+                }
+                // online softmax, rows 2tig (u even) and 2tig+1 (u odd)
+                float mx[2] = {fmaxf(sv[0], sv[2]), fmaxf(sv[1], sv[3])};
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) {
+                    mx[0] = fmaxf(mx[0], __shfl_xor_sync(0xffffffffu, mx[0], o));
+                    mx[1] = fmaxf(mx[1], __shfl_xor_sync(0xffffffffu, mx[1], o));
+                }
+                float alpha[2], mref[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const float mn = fmaxf(m_run[u], mx[u]);
+                    mref[u] = mn == NEG_INF ? 0.f : mn;
+                    alpha[u] = __expf(m_run[u] - mref[u]);
+                    m_run[u] = mn;
+                }
+                float p[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) p[u] = __expf(sv[u] - mref[u & 1]);
+                float ps[2] = {p[0] + p[2], p[1] + p[3]};
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) {
+                    ps[0] += __shfl_xor_sync(0xffffffffu, ps[0], o);
+                    ps[1] += __shfl_xor_sync(0xffffffffu, ps[1], o);
+                }
+                l_run[0] = l_run[0] * alpha[0] + ps[0];
+                l_run[1] = l_run[1] * alpha[1] + ps[1];
+#pragma unroll
+                for (int j = 0; j < C::MT; ++j) {
+                    acc[j][0] *= alpha[0];
+                    acc[j][1] *= alpha[1];
+                    acc[j][2] *= alpha[0];
+                    acc[j][3] *= alpha[1];
+                }
+                // P^T into B fragments: (col gid, rows 2tig..) -> (row gid, cols 2tig..)
+                const uint32_t b0 = movmatrix_trans(pack2<T>(p[0], p[1]));
+                const uint32_t b1 = movmatrix_trans(pack2<T>(p[2], p[3]));
+#pragma unroll
+                for (int j = 0; j < C::MT; ++j) {
+                    const int q = lane >> 3, rr = lane & 7;
+                    const int k = (q >> 1) * 8 + rr;
+                    const int ch = 2 * j + (q & 1);
+                    uint32_t a[4];
+                    ldsm_x4_trans(xs + k * C::XROW + ((ch ^ swz_row<F>(k)) << 4), a[0], a[1], a[2],
+                                  a[3]);
+                    mma_16816<T>(acc[j], a, b0, b1);
+                }
+                __syncwarp();
+                if (p_item < n_items) {
+                    issue(pstage);
+                    p_advance();
+                }
+                cp_async_commit();
+                cstage = cstage + 1 == kGStages ? 0 : cstage + 1;
+                pstage = pstage + 1 == kGStages ? 0 : pstage + 1;
+            }
+        }
+        // ---- epilogue: acc[j] = (feature 16j+gid (+8), rows 2tig, 2tig+1) ----
+        const int slot = A.chunk_slot[chunk];
+        if (slot < 0) {
+            float inv[2] = {l_run[0] > 0.f ? 1.f / l_run[0] : 0.f, l_run[1] > 0.f ? 1.f / l_run[1] : 0.f};
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t row = wrow + 2 * tig + (u & 1);
+                    const int f = 16 * j + gid + 8 * (u >> 1);
+                    if (row < A.n_nodes) A.out[row * A.ldo + h * F + f] = acc[j][u] * inv[u & 1];
+                }
+            if (gid == 0) {
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int64_t row = wrow + 2 * tig + u;
+                    if (row < A.n_nodes) {
+                        if (A.row_max) A.row_max[h * A.n_nodes + row] = m_run[u];
+                        if (A.row_sum) A.row_sum[h * A.n_nodes + row] = l_run[u];
+                    }
+                }
+            }
+        } else {
+            float *pp = A.partial + ((int64_t)slot * A.H + h) * kW * (F + 2);
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int r = 2 * tig + (u & 1);
+                    const int f = 16 * j + gid + 8 * (u >> 1);
+                    pp[r * (F + 2) + f] = acc[j][u];
+                }
+            if (gid == 0) {
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int r = 2 * tig + u;
+                    pp[r * (F + 2) + F] = m_run[u];
+                    pp[r * (F + 2) + F + 1] = l_run[u];
+                }
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// Merge the partials of windows spread over several chunks: one warp per
+// (window, head); the window's chunks are [multi[2i], multi[2i+1]).
+__global__ void k_gat_combine(const int32_t *__restrict__ multi_chunk_begin,
+                              const int32_t *__restrict__ chunk_slot,
+                              const int32_t *__restrict__ chunk_begin,
+                              const int32_t *__restrict__ win, int64_t n_multi, int64_t H,
+                              int64_t F, int64_t n_nodes, const float *__restrict__ partial,
+                              float *__restrict__ out, int64_t ldo, float *row_max,
+                              float *row_sum) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wid >= n_multi * H) return;
+    const int64_t mwin = wid / H, h = wid - mwin * H;
+    const int cb = multi_chunk_begin[2 * mwin], ce = multi_chunk_begin[2 * mwin + 1];
+    const int64_t wrow = (int64_t)win[chunk_begin[cb]] * kW;
+    for (int r = 0; r < kW; ++r) {
+        const int64_t row = wrow + r;
+        if (row >= n_nodes) break;
+        float m = -INFINITY;
+        for (int c = cb; c < ce; ++c) {
+            const float *pp = partial + ((int64_t)chunk_slot[c] * H + h) * kW * (F + 2) + r * (F + 2);
+            m = fmaxf(m, pp[F]);
+        }
+        const float mref = m == -INFINITY ? 0.f : m;
+        float l = 0.f;
+        for (int c = cb; c < ce; ++c) {
+            const float *pp = partial + ((int64_t)chunk_slot[c] * H + h) * kW * (F + 2) + r * (F + 2);
+            l += __expf(pp[F] - mref) * pp[F + 1];
+        }
+        const float inv = l > 0.f ? 1.f / l : 0.f;
+        for (int64_t f = lane; f < F; f += 32) {
+            float a = 0.f;
+            for (int c = cb; c < ce; ++c) {
+                const float *pp =
+                    partial + ((int64_t)chunk_slot[c] * H + h) * kW * (F + 2) + r * (F + 2);
+                a += __expf(pp[F] - mref) * pp[f];
+            }
+            out[row * ldo + h * F + f] = a * inv;
+        }
+        if (lane == 0) {
+            if (row_max) row_max[h * n_nodes + row] = m;
+            if (row_sum) row_sum[h * n_nodes + row] = l;
+        }
+    }
+}
+
+// rows of windows that own no part (and rows past the last window): zero
+__global__ void k_gat_zero_rows(const int32_t *__restrict__ win, int64_t n_parts, int64_t n_nodes,
+                                int64_t H, int64_t F, float *out, int64_t ldo, float *row_max,
+                                float *row_sum) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_w = (n_nodes + kW - 1) / kW;
+    if (w >= n_w) return;
+    int64_t lo = 0, hi = n_parts;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (win[mid] < w) lo = mid + 1; else hi = mid;
+    }
+    if (lo < n_parts && win[lo] == w) return;
+    for (int64_t r = w * kW; r < (w + 1) * kW && r < n_nodes; ++r) {
+        for (int64_t f = lane; f < H * F; f += 32) out[r * ldo + f] = 0.f;
+        if (lane < H) {
+            if (row_max) row_max[lane * n_nodes + r] = -INFINITY;
+            if (row_sum) row_sum[lane * n_nodes + r] = 0.f;
+        }
+    }
+}
+
+// occupancy bitmap from the per-edge slot index
+__global__ void k_slot_mask(const int32_t *__restrict__ edge_slot, int64_t nnz, uint32_t *mask) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnz) return;
+    const int32_t s = edge_slot[e];
+    if (s >= 0) atomicOr(mask + (s >> 5), 1u << (s & 31));
+}
+
+template <typename T, int F, int MODE>
+int run_gat(const GatArgs &P, cudaStream_t st) {
+    using C = GCfg<T, F, MODE>;
+    auto kernel = k_gat_fused<T, F, MODE>;
+    static std::once_flag once;
+    static int prep = ATT_OK;
+    std::call_once(once, [&] {
+        prep = cuda_status(
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
+            "cudaFuncSetAttribute");
+    });
+    if (prep != ATT_OK) return prep;
+    const int64_t items = P.n_chunks * P.H;
+    if (items == 0) return ATT_OK;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGThreads, C::SMEM);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t want = (items + kGWarps - 1) / kGWarps;
+    const int64_t cap = (int64_t)sm_count() * per_sm;
+    kernel<<<(unsigned)(want < cap ? want : cap), kGThreads, C::SMEM, st>>>(P);
+    return launch_status("k_gat_fused");
+}
+
+template <typename T, int MODE>
+int dispatch_gat_f(const GatArgs &P, cudaStream_t st) {
+    switch (P.F) {
+        case 32: return run_gat<T, 32, MODE>(P, st);
+        case 64: return run_gat<T, 64, MODE>(P, st);
+        case 128: return run_gat<T, 128, MODE>(P, st);
+        default:
+            set_error("fused GAT supports F in {32, 64, 128}, got %lld", (long long)P.F);
+            return ATT_ERR_UNSUPPORTED;
+    }
+}
+
+}  // namespace
+}  // namespace att
+
+using namespace att;
+
+extern "C" int att_slot_mask(const int32_t *edge_slot, int64_t nnz, uint32_t *mask,
+                             int64_t n_words, void *stream) {
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n_words > 0) {
+        ATT_CHECK(mask != nullptr, ATT_ERR_INVALID, "null mask");
+        ATT_CUDA(cudaMemsetAsync(mask, 0, (size_t)n_words * 4, st), "memset mask");
+    }
+    if (nnz == 0) return ATT_OK;
+    ATT_CHECK(edge_slot != nullptr, ATT_ERR_INVALID, "null edge_slot");
+    k_slot_mask<<<(unsigned)((nnz + 255) / 256), 256, 0, st>>>(edge_slot, nnz, mask);
+    return launch_status("k_slot_mask");
+}
+
+extern "C" int att_gat_forward(const int32_t *rowptr, const int32_t *col, const uint32_t *slot_mask,
+                               const int32_t *window_of_part, int64_t n_parts,
+                               const int32_t *chunk_begin, const int32_t *chunk_slot,
+                               int64_t n_chunks, const int32_t *multi_chunk_begin,
+                               int64_t n_multi, int window, int wide, const void *Xp, int x_dtype,
+                               int64_t n_nodes, int64_t n_heads, int64_t F, int64_t ldx, int mode,
+                               const float *s0, const float *s1, float slope, float *out,
+                               int64_t ldo, float *row_max, float *row_sum, float *partial,
+                               int32_t *err_flag, void *stream) {
+    clear_error();
+    ATT_CHECK(window == kW, ATT_ERR_UNSUPPORTED, "fused GAT needs 8-row windows");
+    ATT_CHECK(wide == 4 || wide == 8 || wide == 16, ATT_ERR_UNSUPPORTED, "wide must be 4, 8 or 16");
+    ATT_CHECK(mode == 0 || mode == 1, ATT_ERR_INVALID, "mode must be 0 (dot) or 1 (additive)");
+    ATT_CHECK(x_dtype == ATT_F16 || x_dtype == ATT_BF16, ATT_ERR_UNSUPPORTED,
+              "fused GAT takes fp16 or bf16 features");
+    ATT_CHECK(n_heads > 0 && n_heads <= 32 && F > 0, ATT_ERR_INVALID, "bad heads / features");
+    ATT_CHECK(ldx % 8 == 0 && ((uintptr_t)Xp & 15) == 0 && ldx >= n_heads * F, ATT_ERR_UNSUPPORTED,
+              "X' rows must be 16-byte aligned with ldx >= heads*F");
+    ATT_CHECK(ldo >= n_heads * F, ATT_ERR_INVALID, "ldo < heads*F");
+    ATT_CHECK(mode == 0 || (s0 && s1), ATT_ERR_INVALID, "additive mode needs node scores");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n_nodes == 0) return ATT_OK;
+    {
+        const int64_t threads = (n_nodes + kW - 1) / kW * 32;
+        k_gat_zero_rows<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+            window_of_part, n_parts, n_nodes, n_heads, F, out, ldo, row_max, row_sum);
+        int s = launch_status("k_gat_zero_rows");
+        if (s != ATT_OK) return s;
+    }
+    if (n_chunks == 0) return ATT_OK;
+    ATT_CHECK(rowptr && col && slot_mask && window_of_part && chunk_begin && chunk_slot,
+              ATT_ERR_INVALID, "null format pointer");
+    ATT_CHECK(n_multi == 0 || (partial && multi_chunk_begin), ATT_ERR_INVALID,
+              "split windows need the partial buffer");
+    GatArgs P{rowptr, col, window_of_part, slot_mask, chunk_begin, chunk_slot, n_chunks, wide, Xp,
+              n_nodes, n_heads, F, ldx, mode, s0, s1, slope, out, ldo, row_max, row_sum, partial,
+              err_flag};
+    int s;
+    if (x_dtype == ATT_F16) s = mode == 0 ? dispatch_gat_f<__half, 0>(P, st) : dispatch_gat_f<__half, 1>(P, st);
+    else s = mode == 0 ? dispatch_gat_f<__nv_bfloat16, 0>(P, st) : dispatch_gat_f<__nv_bfloat16, 1>(P, st);
+    if (s != ATT_OK) return s;
+    if (n_multi > 0) {
+        const int64_t threads = n_multi * n_heads * 32;
+        k_gat_combine<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+            multi_chunk_begin, chunk_slot, chunk_begin, window_of_part, n_multi, n_heads, F,
+            n_nodes, partial, out, ldo, row_max, row_sum);
+        s = launch_status("k_gat_combine");
+    }
+    return s;
+}

@@ -242,6 +242,40 @@ ATT_API int att_rowsum(const int32_t *rowptr, const int32_t *map,
                    int64_t v_stride_e, int64_t n_heads, float *out, int64_t out_stride_h,
                    int64_t out_stride_n, int64_t m_out, void *stream);
 
+/* ======================================================================
+ * Fused GAT attention layer (SDDMM -> LeakyReLU -> edge softmax -> SpMM in
+ * one pass, no per-edge intermediates).  Replaces the reference's op chain of
+ * end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198 (att_fp16_h_nnz,
+ * leakyrelu, exp, spmm_fp16_h_m_rowsum, spmm_fp16_h_m, div).
+ * ====================================================================== */
+
+/* Occupancy bitmap of a block format: bit s set iff slot s holds an edge
+ * (from att_block_fill's edge_slot).  mask has n_words = ceil(n_slots/32)
+ * words and is cleared first. */
+ATT_API int att_slot_mask(const int32_t *edge_slot, int64_t nnz, uint32_t *mask,
+                   int64_t n_words, void *stream);
+
+/* out[i][h*F + f] = sum_j softmax_j(LeakyReLU(e_ij)) X'[j][h*F + f] over the
+ * edges (i, j) of row i, per head h, with
+ *   mode 0: e_ij = X'_i . X'_j (SDDMM of X' X'^T masked to the edges)
+ *   mode 1: e_ij = s0[h][i] + s1[h][j] (GAT's additive a0/a1 scores).
+ * Row max and sum stay fp32.  Work items are chunks of consecutive parts of
+ * one window: chunk c covers parts [chunk_begin[c], chunk_begin[c+1]);
+ * chunk_slot[c] = -1 if the chunk covers its whole window, else its row in
+ * `partial` ([n_slots][n_heads][8][F+2] fp32 scratch); multi_chunk_begin holds
+ * (first, end) chunk pairs of the n_multi windows spread over several chunks.
+ * row_max / row_sum ([n_heads][n_nodes], may be NULL) receive the softmax
+ * statistics for the backward pass.  8-row windows, F in {32, 64, 128},
+ * fp16 or bf16 X'.  Every row < n_nodes of out is written. */
+ATT_API int att_gat_forward(const int32_t *rowptr, const int32_t *col, const uint32_t *slot_mask,
+                   const int32_t *window_of_part, int64_t n_parts,
+                   const int32_t *chunk_begin, const int32_t *chunk_slot, int64_t n_chunks,
+                   const int32_t *multi_chunk_begin, int64_t n_multi, int window, int wide,
+                   const void *Xp, int x_dtype, int64_t n_nodes, int64_t n_heads, int64_t F,
+                   int64_t ldx, int mode, const float *s0, const float *s1, float slope,
+                   float *out, int64_t ldo, float *row_max, float *row_sum, float *partial,
+                   int32_t *err_flag, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -316,3 +316,13 @@ def spmm_cpu_fp32(A, X):
     """Y = A X with torch.sparse on the host cores (fp32)."""
     import torch
     return torch.sparse.mm(A, X)
+
+
+def gat_dot_layer_fp64(rowptr, col, Xp, n_out, slope=0.2):
+    """GAT layer with dot-product logits per head (BASELINE's GAT-layer
+    workload): e_ij = Xp_i . Xp_j -> LeakyReLU -> row softmax -> sum_j p_ij Xp_j.
+    Xp [h, M, F]."""
+    e = sddmm_fp64(rowptr, col, Xp, Xp)
+    e = np.where(e > 0, e, slope * e)
+    p = edge_softmax_fp64(rowptr, e)
+    return spmm_edge_fp64(rowptr, col, p, Xp, n_out)

@@ -1,0 +1,64 @@
+"""Fused GAT layer (SDDMM -> LeakyReLU -> edge softmax -> SpMM in one kernel)
+vs the FP64 oracle; tolerance 1e-2 normwise relative (fp16/bf16 features,
+fp32 softmax statistics)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _graph(n, deg, gamma, seed, hub=False):
+    from att_gb300 import graphs
+    rp, col = graphs.chung_lu(n, deg, gamma, seed=seed, max_deg_frac=0.9 if hub else 0.5)
+    return rp, col
+
+
+@pytest.mark.parametrize("mode", ["dot", "add"])
+@pytest.mark.parametrize("F,H", [(64, 1), (32, 4), (128, 2)])
+@pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16])
+def test_fused_gat_vs_fp64(cuda, mode, F, H, dtype):
+    from att_gb300 import gat
+    n = 1500
+    rp, col = _graph(n, 40, 1.9, seed=7, hub=True)  # hub windows -> split chunks
+    G = gat.GATGraph(rp, col, parts_per_chunk=2)
+    assert G.n_multi > 0
+    g = torch.Generator().manual_seed(F + H)
+    Xp = ((torch.rand(n, H * F, generator=g) * 2 - 1) * (0.6 if mode == "dot" else 1.0))
+    X3 = Xp.view(n, H, F).permute(1, 0, 2).double().numpy()
+    Xq = Xp.to(dtype)
+    X3q = Xq.view(n, H, F).permute(1, 0, 2).double().numpy()
+    rpn, coln = rp.numpy(), col.numpy()
+    if mode == "dot":
+        out, rmax, rsum = G.attention(Xq.cuda(), n_heads=H, mode=gat.MODE_DOT)
+        ref = oracle.gat_dot_layer_fp64(rpn, coln, X3q, n)
+    else:
+        a0 = (torch.rand(H, F, generator=g) - 0.5)
+        a1 = (torch.rand(H, F, generator=g) - 0.5)
+        s0 = torch.einsum("hmf,hf->hm", torch.from_numpy(X3q), a0.double()).float()
+        s1 = torch.einsum("hmf,hf->hm", torch.from_numpy(X3q), a1.double()).float()
+        out, rmax, rsum = G.attention(Xq.cuda(), n_heads=H, mode=gat.MODE_ADD, s0=s0.cuda(),
+                                      s1=s1.cuda())
+        ref = oracle.gat_layer_fp64(rpn, coln, X3q, a0.numpy()[:, None, :], a1.numpy()[:, None, :], n)
+    got = out.view(n, H, F).permute(1, 0, 2).cpu().numpy()
+    err = oracle.rel_err(got, ref)
+    assert err <= 1e-2, err
+    # softmax statistics: sum_j exp(e_ij - m_i) = l_i
+    assert torch.isfinite(rmax[:, :n]).all() and (rsum[:, :n] >= 1.0 - 1e-3).all()
+
+
+def test_fused_gat_empty_rows_and_tail(cuda):
+    from att_gb300 import gat, graphs
+    rp, col = graphs.random_csr(203, 203, 9, seed=3, empty_frac=0.4, hub_rows=1, hub_len=180)
+    rp = graphs.pad_rows(torch.from_numpy(rp), 8)
+    G = gat.GATGraph(rp, torch.from_numpy(col), parts_per_chunk=1)
+    n = rp.shape[0] - 1
+    Xp = torch.rand(n, 64, generator=torch.Generator().manual_seed(1)).half()
+    out, rmax, rsum = G.attention(Xp.cuda())
+    X3 = Xp.double().numpy()[None]
+    ref = oracle.gat_dot_layer_fp64(rp.numpy(), col, X3, n)
+    assert oracle.rel_err(out.cpu().numpy()[None], ref) <= 1e-2
+    empty = (rp[1:] - rp[:-1]) == 0
+    assert torch.all(out.cpu()[empty] == 0)
