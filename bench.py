@@ -113,15 +113,28 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
+def distinct_window_columns(rowptr, col, window=8):
+    """Number of distinct (row // window, column) pairs of a host CSR: the X
+    rows a blocked kernel gathers."""
+    import torch
+    rowptr = torch.as_tensor(rowptr).long()
+    n = rowptr.numel() - 1
+    rows = torch.repeat_interleave(torch.arange(n), rowptr[1:] - rowptr[:-1])
+    key = (rows // window) * (int(col.max()) + 1 if col.numel() else 1) + torch.as_tensor(col).long()
+    return int(torch.unique(key).numel())
+
+
 class SpmmProducts:
     """Blocked FP16 SpMM on the 2.45M-node power-law graph."""
     name = "spmm_products_fp16"
     unit = "GB/s"
     N, MEAN_DEG, GAMMA, SEED, F, F_REAL = 2_449_029, 25, 2.2, 2, 128, 100
 
-    def __init__(self, device, scale=1.0):
+    e2e_api = "SpMM_sr_bcrs.forward_fp16_gnn"
+
+    def __init__(self, device, scale=1.0, light=False):
         import torch
-        from att_gb300 import graphs, ops
+        from att_gb300 import graphs
         self.torch = torch
         n = int(self.N * scale)
         self.n = n
@@ -131,16 +144,21 @@ class SpmmProducts:
         deg = graphs.gcn_degree(rp, torch.float16)
         deg = torch.where(torch.isfinite(deg), deg, torch.zeros_like(deg))
         self.deg = deg
-        self.fmt = ops.block_convert(rp, col, deg, window=8, wide=8, part=32)
         g = torch.Generator(device=device)
         g.manual_seed(self.SEED)
         X = torch.rand(n, self.F, generator=g, device=device, dtype=torch.float32) * 2 - 1
         X[:, self.F_REAL:] = 0
         self.X = X.half()
+        self.nnz = int(col.shape[0])
+        if light:  # CSR and features only: no kernel of this package runs
+            self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz,
+                           "features": self.F, "real_features": self.F_REAL}
+            return
+        from att_gb300 import ops
+        self.fmt = ops.block_convert(rp, col, deg, window=8, wide=8, part=32)
         self.Y = torch.empty(n, self.F, device=device, dtype=torch.float32)
         f = self.fmt
         real = (f.rowptr[1::2] - f.rowptr[0:-1:2]).sum().item()
-        self.nnz = int(col.shape[0])
         self.U = int(real)  # distinct (8-row window, column) pairs = gathered X rows
         F = self.F
         self.bytes_alg = 4 * (n + 1) + self.nnz * (4 + 2) + self.U * F * 2 + n * F * 4
@@ -203,17 +221,120 @@ class SpmmProducts:
         d = self.deg.cpu().float()
         vals = (d[ridx] * d[col]).half().float()
         X = self.X.float().cpu()
-        f = self.fmt
-        wins = f.window_of_part.cpu()
-        rr = f.rowptr.cpu()
-        sel = wins < (rows // 8)
-        U = int((rr[1::2] - rr[0:-1:2])[sel].sum())
+        U = distinct_window_columns(rp, col)
         nnz = int(col.shape[0])
         b = 4 * (rows + 1) + nnz * (4 + 2) + U * self.F * 2 + rows * self.F * 4
         return rp, col, vals, X, rows, b
 
 
-WORKLOADS = {SpmmProducts.name: SpmmProducts}
+class GatReddit:
+    """One GAT layer forward on the 232,965-node graph: X' = X W (cuBLAS), then
+    the fused SDDMM -> LeakyReLU -> edge softmax -> SpMM kernel."""
+    name = "gat_reddit_fp16"
+    unit = "GB/s"
+    N, MEAN_DEG, GAMMA, SEED, F = 232_965, 490, 1.9, 1, 64
+
+    e2e_api = "att_gb300.gat.GATGraph.attention (C ABI att_gat_forward) after torch.mm"
+
+    def __init__(self, device, scale=1.0, light=False):
+        import torch
+        from att_gb300 import graphs
+        self.torch = torch
+        n = max(int(self.N * scale), 64)
+        self.n = n
+        rp, col = graphs.chung_lu(n, self.MEAN_DEG * min(1.0, scale ** 0.5), self.GAMMA,
+                                  self.SEED, device=device)
+        self.rowptr, self.colidx = rp, col
+        g = torch.Generator(device=device)
+        g.manual_seed(self.SEED)
+        F = self.F
+        self.X = (torch.rand(n, F, generator=g, device=device) * 2 - 1).half()
+        a = (6.0 / (F + F)) ** 0.5  # Glorot-uniform bound
+        self.W = ((torch.rand(F, F, generator=g, device=device) * 2 - 1) * a).half()
+        self.nnz = int(col.shape[0])
+        if light:  # CSR and features only: no kernel of this package runs
+            self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz, "features": F}
+            return
+        from att_gb300 import gat
+        self.G = gat.GATGraph(rp, col)
+        self.out = torch.empty(n, F, device=device, dtype=torch.float32)
+        f = self.G.fmt
+        self.U = int((f.rowptr[1::2] - f.rowptr[0:-1:2]).sum().item())
+        # fused kernel: CSR-granular structure + query rows + gathered rows + output
+        self.bytes_fused = 4 * (n + 1) + 4 * self.nnz + n * F * 2 + self.U * F * 2 + n * F * 4
+        self.bytes_alg = self.bytes_fused + 2 * n * F * 2  # + the projection's X read, X' write
+        self.flops = 2 * n * F * F + 4 * self.nnz * F
+        self.launches_per_step = 2 + (1 if self.G.n_multi else 0)
+        self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz, "features": F,
+                       "heads": 1, "gamma": self.GAMMA, "mean_degree": self.MEAN_DEG,
+                       "seed": self.SEED, "format": "window 8, wide 8, partSize 32",
+                       "parts": f.n_parts, "condensed_cols": f.n_condensed,
+                       "gathered_rows_U8": self.U, "chunks": self.G.n_chunks,
+                       "split_windows": self.G.n_multi, "x_dtype": "fp16", "out_dtype": "fp32",
+                       "attention": "dot-product logits (X W)(X W)^T on the edges, "
+                                    "LeakyReLU 0.2, row softmax with fp32 max/sum",
+                       "l2": "X' (30 MB) is L2-resident; structure arrays are larger than L2"}
+
+    kernel_name = "att_gat_forward (k_gat_zero_rows + k_gat_fused + k_gat_combine)"
+
+    def step(self):
+        Xp = self.torch.mm(self.X, self.W)
+        self.G.attention(Xp, out=self.out, stats=False)
+
+    def kernel_step(self):
+        """the dominant kernel launch alone (for the roofline timing)"""
+        self.G.attention(self.Xp, out=self.out, stats=False)
+
+    def prepare_kernel(self):
+        self.Xp = self.torch.mm(self.X, self.W)
+
+    def e2e_setup(self):
+        torch = self.torch
+        self.Xh = self.X.cpu().pin_memory()
+        self.Wh = self.W.cpu().pin_memory()
+        self.Oh = torch.empty(self.n, self.F, dtype=torch.float32).pin_memory()
+        self.h2d = self.Xh.numel() * 2 + self.Wh.numel() * 2
+        self.d2h = self.Oh.numel() * 4
+
+    def e2e_step(self):
+        X = self.Xh.to("cuda", non_blocking=True)
+        W = self.Wh.to("cuda", non_blocking=True)
+        out, _, _ = self.G.attention(self.torch.mm(X, W), stats=False)
+        self.Oh.copy_(out, non_blocking=True)
+
+    def check(self):
+        """Size-independent property at full size: every output row is a convex
+        combination of its neighbours' X' rows, so it lies within their
+        per-feature min/max (checked on a sample of rows against the CSR)."""
+        torch = self.torch
+        Xp = torch.mm(self.X, self.W).float()
+        out, rmax, rsum = self.G.attention(Xp.half())
+        rp = self.rowptr.long()
+        worst = 0.0
+        for r in torch.linspace(0, self.n - 1, 64).long().tolist():
+            nb = self.colidx[rp[r]:rp[r + 1]].long()
+            if nb.numel() == 0:
+                continue
+            lo = Xp[nb].min(0).values
+            hi = Xp[nb].max(0).values
+            span = (hi - lo).abs().max().clamp_min(1e-6)
+            over = torch.clamp(out[r] - hi, min=0).max() + torch.clamp(lo - out[r], min=0).max()
+            worst = max(worst, float(over / span))
+        return worst
+
+    def cpu_sample(self, max_rows):
+        torch = self.torch
+        rows = min(max_rows, self.n)
+        rp = self.rowptr[: rows + 1].cpu().long()
+        col = self.colidx[: int(rp[-1])].cpu().long()
+        Xp = torch.mm(self.X.float().cpu(), self.W.float().cpu())
+        U = distinct_window_columns(rp, col)
+        nnz = int(col.shape[0])
+        b = 4 * (rows + 1) + 4 * nnz + rows * self.F * 2 + U * self.F * 2 + rows * self.F * 4
+        return rp, col, Xp, rows, b
+
+
+WORKLOADS = {SpmmProducts.name: SpmmProducts, GatReddit.name: GatReddit}
 DEFAULT_WORKLOAD = SpmmProducts.name
 
 
@@ -231,22 +352,31 @@ def cpu_baseline(wl, budget_s=12.0):
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
     rows = max(8, wl.n // 64)
-    rp, col, vals, X, rows, b = wl.cpu_sample(rows)
-    A = orc.csr_fp32(rp, col, vals, X.shape[0])
+    if isinstance(wl, GatReddit):
+        rp, col, Xp, rows, b = wl.cpu_sample(rows)
+        run = lambda: orc.gat_dot_layer_cpu_fp32(rp, col, Xp)  # noqa: E731
+        what = "GAT layer (dot logits, LeakyReLU, softmax, aggregation) in torch fp32"
+        F = Xp.shape[1]
+    else:
+        rp, col, vals, X, rows, b = wl.cpu_sample(rows)
+        A = orc.csr_fp32(rp, col, vals, X.shape[0])
+        run = lambda: orc.spmm_cpu_fp32(A, X)  # noqa: E731
+        what = "torch.sparse CSR fp32 SpMM"
+        F = X.shape[1]
     t0 = time.perf_counter()
-    orc.spmm_cpu_fp32(A, X)
+    run()
     one = time.perf_counter() - t0
     reps = max(3, min(50, int(budget_s / max(one, 1e-3))))
     ts = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        orc.spmm_cpu_fp32(A, X)
+        run()
         ts.append(time.perf_counter() - t0)
     ts.sort()
     med = ts[len(ts) // 2]
     return {"value": b / med / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": "first %d rows of the same graph (%d edges), torch.sparse CSR fp32 SpMM x "
-                      "[N,%d], median of %d runs" % (rows, int(col.shape[0]), X.shape[1], reps),
+            "sample": "first %d rows of the same graph (%d edges), %s, F=%d, median of %d runs"
+                      % (rows, int(col.shape[0]), what, F, reps),
             "ms_per_sample": med * 1e3}
 
 
@@ -257,7 +387,7 @@ def run_reference(args):
     import torch
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     t_setup = time.time()
-    wl = WORKLOADS[args.workload](dev, scale=args.scale)
+    wl = WORKLOADS[args.workload](dev, scale=args.scale, light=True)
     base = cpu_baseline(wl, budget_s=max(3.0, 20.0 / max(1, args.steps + args.warmup)))
     line = {"metric": METRIC, "impl": "reference", "value": base["value"], "unit": wl.unit,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -315,16 +445,24 @@ def main():
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     t_all0 = torch.cuda.Event(enable_timing=True)
     t_all1 = torch.cuda.Event(enable_timing=True)
     t_all0.record(stream)
     for k in range(args.steps):
-        ev[k][0].record(stream)
         wl.step()
-        ev[k][1].record(stream)
     t_all1.record(stream)
+    torch.cuda.synchronize()
+    # dominant kernel alone, per launch, for the roofline
+    kernel_step = getattr(wl, "kernel_step", wl.step)
+    if hasattr(wl, "prepare_kernel"):
+        wl.prepare_kernel()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        kernel_step()
+        ev[k][1].record(stream)
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -359,7 +497,8 @@ def main():
     e2e_ms = float(e2e_ms_t.item())
 
     peak, peak_kind = peaks()
-    achieved = wl.bytes_alg / (avg_launch_ms * 1e-3) / 1e9
+    kbytes = getattr(wl, "bytes_fused", wl.bytes_alg)
+    achieved = kbytes / (avg_launch_ms * 1e-3) / 1e9
     line = None
     if rank == 0:
         base = None
@@ -367,18 +506,20 @@ def main():
             base = cpu_baseline(wl)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                "kernel": "att_spmm (k_zero_uncovered + k_spmm16), avg of %d launches" % args.steps,
-                "bytes_per_launch": wl.bytes_alg}
+                "kernel": getattr(wl, "kernel_name", "att_spmm (k_zero_uncovered + k_spmm16)")
+                          + ", avg of %d launches" % args.steps,
+                "bytes_per_launch": kbytes}
         line = {"metric": METRIC, "value": value, "unit": wl.unit, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f16", "data": "synthetic", "config": dict(wl.config),
+                "workload_ms_per_step": ms_per_step,
                 "roofline": roof,
                 "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
                                  if base else None),
                 "e2e": {"value": world * wl.bytes_alg / (e2e_ms * 1e-3) / 1e9, "unit": wl.unit,
                         "h2d_bytes_per_step": wl.h2d, "d2h_bytes_per_step": wl.d2h,
-                        "ms_per_step": e2e_ms, "api": "SpMM_sr_bcrs.forward_fp16_gnn"},
+                        "ms_per_step": e2e_ms, "api": wl.e2e_api},
                 "gpu_launches": wl.launches_per_step * args.steps,
                 "clocks": clocks,
                 "gflops": world * wl.flops / (ms_per_step * 1e-3) / 1e9,

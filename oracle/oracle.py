@@ -326,3 +326,23 @@ def gat_dot_layer_fp64(rowptr, col, Xp, n_out, slope=0.2):
     e = np.where(e > 0, e, slope * e)
     p = edge_softmax_fp64(rowptr, e)
     return spmm_edge_fp64(rowptr, col, p, Xp, n_out)
+
+
+def gat_dot_layer_cpu_fp32(rowptr, col, Xp, slope=0.2):
+    """CPU fp32 restatement (torch, all host threads) of the GAT layer with dot
+    logits, for the CPU baseline: e = Xp_i . Xp_j on the edges, LeakyReLU,
+    row softmax (max-subtracted), weighted sum of neighbour rows."""
+    import torch
+    rowptr = torch.as_tensor(rowptr).long()
+    col = torch.as_tensor(col).long()
+    n = rowptr.numel() - 1
+    rows = torch.repeat_interleave(torch.arange(n), rowptr[1:] - rowptr[:-1])
+    Xr = Xp[rows]
+    Xc = Xp[col]
+    e = (Xr * Xc).sum(1)
+    e = torch.nn.functional.leaky_relu(e, slope)
+    m = torch.full((n,), float("-inf")).scatter_reduce(0, rows, e, "amax")
+    p = torch.exp(e - m[rows])
+    l = torch.zeros(n).index_add_(0, rows, p)
+    out = torch.zeros(n, Xp.shape[1]).index_add_(0, rows, p[:, None] * Xc)
+    return out / l.clamp_min(1e-30)[:, None]
