@@ -58,6 +58,10 @@ _SIGNATURES = {
                                  _c_i64, _c_int, _c_int, _c_vp, _c_int, _c_i64, _c_i64, _c_i64,
                                  _c_i64, _c_int, _c_vp, _c_vp, ctypes.c_float, _c_vp, _c_i64,
                                  _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "att_gat_backward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_vp,
+                                  _c_vp, _c_vp, _c_int, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64, _c_vp,
+                                  _c_vp, _c_vp, _c_vp, _c_vp, ctypes.c_float, _c_vp, _c_i64,
+                                  _c_vp, _c_vp, _c_vp, _c_vp]),
 }
 
 _lib = None

@@ -40,6 +40,17 @@ __device__ __forceinline__ uint32_t movmatrix_trans(uint32_t x) {
 }
 
 template <typename T>
+__device__ __forceinline__ float2 unpack2(uint32_t v);
+template <>
+__device__ __forceinline__ float2 unpack2<__half>(uint32_t v) {
+    return __half22float2(*reinterpret_cast<__half2 *>(&v));
+}
+template <>
+__device__ __forceinline__ float2 unpack2<__nv_bfloat16>(uint32_t v) {
+    return __bfloat1622float2(*reinterpret_cast<__nv_bfloat162 *>(&v));
+}
+
+template <typename T>
 __device__ __forceinline__ uint32_t pack2(float lo, float hi);
 template <>
 __device__ __forceinline__ uint32_t pack2<__half>(float lo, float hi) {
@@ -100,7 +111,10 @@ struct GCfg {
     static constexpr int MT = F / 16;
 };
 
-template <typename T, int F, int MODE>
+// PSPLIT: aggregate with P as a hi + lo pair of 16-bit values (fp32-accurate
+// output); the training path needs it so that dout . out matches the
+// backward's recomputed probabilities.
+template <typename T, int F, int MODE, bool PSPLIT>
 __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     using C = GCfg<T, F, MODE>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -320,8 +334,15 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                     acc[j][3] *= alpha[1];
                 }
                 // P^T into B fragments: (col gid, rows 2tig..) -> (row gid, cols 2tig..)
-                const uint32_t b0 = movmatrix_trans(pack2<T>(p[0], p[1]));
-                const uint32_t b1 = movmatrix_trans(pack2<T>(p[2], p[3]));
+                const uint32_t h01 = pack2<T>(p[0], p[1]), h23 = pack2<T>(p[2], p[3]);
+                const uint32_t b0 = movmatrix_trans(h01);
+                const uint32_t b1 = movmatrix_trans(h23);
+                uint32_t bl0 = 0, bl1 = 0;
+                if constexpr (PSPLIT) {
+                    const float2 r01 = unpack2<T>(h01), r23 = unpack2<T>(h23);
+                    bl0 = movmatrix_trans(pack2<T>(p[0] - r01.x, p[1] - r01.y));
+                    bl1 = movmatrix_trans(pack2<T>(p[2] - r23.x, p[3] - r23.y));
+                }
 #pragma unroll
                 for (int j = 0; j < C::MT; ++j) {
                     const int q = lane >> 3, rr = lane & 7;
@@ -331,6 +352,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                     ldsm_x4_trans(xs + k * C::XROW + ((ch ^ swz_row<F>(k)) << 4), a[0], a[1], a[2],
                                   a[3]);
                     mma_16816<T>(acc[j], a, b0, b1);
+                    if constexpr (PSPLIT) mma_16816<T>(acc[j], a, bl0, bl1);
                 }
                 __syncwarp();
                 if (p_item < n_items) {
@@ -464,10 +486,10 @@ __global__ void k_slot_mask(const int32_t *__restrict__ edge_slot, int64_t nnz, 
     if (s >= 0) atomicOr(mask + (s >> 5), 1u << (s & 31));
 }
 
-template <typename T, int F, int MODE>
+template <typename T, int F, int MODE, bool PSPLIT>
 int run_gat(const GatArgs &P, cudaStream_t st) {
     using C = GCfg<T, F, MODE>;
-    auto kernel = k_gat_fused<T, F, MODE>;
+    auto kernel = k_gat_fused<T, F, MODE, PSPLIT>;
     static std::once_flag once;
     static int prep = ATT_OK;
     std::call_once(once, [&] {
@@ -489,12 +511,326 @@ int run_gat(const GatArgs &P, cudaStream_t st) {
 
 template <typename T, int MODE>
 int dispatch_gat_f(const GatArgs &P, cudaStream_t st) {
+    const bool split = P.row_sum != nullptr;  // statistics requested: training path
     switch (P.F) {
-        case 32: return run_gat<T, 32, MODE>(P, st);
-        case 64: return run_gat<T, 64, MODE>(P, st);
-        case 128: return run_gat<T, 128, MODE>(P, st);
+        case 32: return split ? run_gat<T, 32, MODE, true>(P, st) : run_gat<T, 32, MODE, false>(P, st);
+        case 64: return split ? run_gat<T, 64, MODE, true>(P, st) : run_gat<T, 64, MODE, false>(P, st);
+        case 128: return split ? run_gat<T, 128, MODE, true>(P, st) : run_gat<T, 128, MODE, false>(P, st);
         default:
             set_error("fused GAT supports F in {32, 64, 128}, got %lld", (long long)P.F);
+            return ATT_ERR_UNSUPPORTED;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Backward of the additive GAT layer, fused.  With the forward's row max m and
+// sum l saved, and c_i = dout_i . out_i, every edge term is local:
+//   p_ij  = exp(LeakyReLU(s0_i + s1_j) - m_i) / l_i
+//   dp_ij = dout_i . X'_j
+//   dz_ij = p_ij (dp_ij - c_i) LeakyReLU'(s0_i + s1_j)
+//   dX'_j += p_ij dout_i      (the SpMM adjoint)
+//   ds1_j += dz_ij,  ds0_i += dz_ij
+// One pass over the block format of the TRANSPOSED graph: window rows are the
+// j's, condensed columns the i's.  Per 16 columns: the dout rows of the i's
+// are gathered (cp.async ring) and feed dp (mma, K = F) and the adjoint
+// product (mma after a movmatrix transpose of p); ds1 is a register row sum,
+// ds0 one atomic add per (window, column).  All outputs are accumulated with
+// red.global.add into zeroed buffers.
+struct GatBwdArgs {
+    const int32_t *rowptr, *col, *win;
+    const uint32_t *mask;
+    int64_t n_parts;
+    int wide;
+    const void *Xp;    // X'[j][h*F + f]  (rows of the transposed windows)
+    const void *dout;     // dout[i][h*F + f] (gathered)
+    const void *dout_lo;  // dout - dout (rounded), same layout, or null
+    int64_t n_nodes, H, F, ldx, ldd;
+    const float *s0, *s1, *m, *l, *c;  // [H][n_nodes]
+    float slope;
+    float *dXp;  // [n_nodes][H*F] fp32, ld ldg
+    int64_t ldg;
+    float *ds0, *ds1;  // [H][n_nodes]
+    int32_t *err;
+};
+
+template <typename T, int F, bool SPLIT>
+struct BCfg {
+    static constexpr int XROW = F * 2;
+    static constexpr int TILE = 16 * XROW;
+    static constexpr int XSTAGE = (SPLIT ? 2 : 1) * TILE;
+    static constexpr int MSTAGE = 16;
+    static constexpr int CSTAGE = 4 * 64;  // s0, m, l, c of the 16 columns
+    static constexpr int STAGE = XSTAGE + MSTAGE + CSTAGE;
+    static constexpr int WARP_SMEM = kGStages * STAGE;
+    static constexpr int SMEM = kGWarps * WARP_SMEM;
+    static constexpr int CPR = XROW / 16;
+    static constexpr int PASSES = (16 * CPR + 31) / 32;
+    static constexpr int MT = F / 16;
+};
+
+template <typename T, int F, bool SPLIT>
+__global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
+    using C = BCfg<T, F, SPLIT>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
+    const unsigned char *sgen = smem + warp * C::WARP_SMEM;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int64_t n_items = A.n_parts * A.H;
+    const int64_t stride = (int64_t)gridDim.x * kGWarps;
+    const T *Xq = (const T *)A.Xp;
+    const T *D = (const T *)A.dout;
+    const T *DL = (const T *)A.dout_lo;
+
+    int64_t p_item = (int64_t)blockIdx.x * kGWarps + warp;
+    int64_t p_h = 0;
+    int p_start = 0, p_nreal = 0, p_pend = 0, p_step = 0;
+    auto p_load = [&]() {
+        while (p_item < n_items) {
+            const int64_t part = p_item / A.H;
+            p_h = p_item - part * A.H;
+            p_start = A.rowptr[2 * part];
+            const int e = A.rowptr[2 * part + 1];
+            p_pend = A.rowptr[2 * part + 2];
+            p_nreal = e > p_start ? e - p_start : 0;
+            if ((p_start % A.wide) != 0 || (p_pend % A.wide) != 0 || p_pend < p_start + p_nreal) {
+                if (A.err) atomicOr(A.err, 2);
+                p_nreal = 0;
+            }
+            p_step = 0;
+            if (p_nreal > 0) return;
+            p_item += stride;
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * C::STAGE;
+        const uint32_t ms = xs + C::XSTAGE;
+        const uint32_t cs = ms + C::MSTAGE;
+        const int c0 = p_step * 16;
+        int myc = -1;
+        if (c0 + (lane & 15) < p_nreal) myc = A.col[p_start + c0 + (lane & 15)];
+        if (myc >= A.n_nodes || myc < -1) {
+            if (A.err) atomicOr(A.err, 1);
+            myc = -1;
+        }
+#pragma unroll
+        for (int i = 0; i < C::PASSES; ++i) {
+            const int idx = i * 32 + lane;
+            const int r = idx / C::CPR, ch = idx % C::CPR;
+            const int cidx = __shfl_sync(0xffffffffu, myc, r & 15);
+            if (idx < 16 * C::CPR) {
+                const bool ok = cidx >= 0;
+                const int64_t o = (int64_t)cidx * A.ldd + p_h * F + ch * 8;
+                const uint32_t d = r * C::XROW + ((ch ^ swz_row<F>(r)) << 4);
+                cp_async16(xs + d, ok ? D + o : D, ok ? 16 : 0);
+                if constexpr (SPLIT) cp_async16(xs + C::TILE + d, ok ? DL + o : DL, ok ? 16 : 0);
+            }
+        }
+        if (lane < 2) {
+            const bool ok = c0 + 8 * lane < p_pend - p_start;
+            const int64_t bit0 = (int64_t)(p_start + c0 + 8 * lane) * kW;
+            cp_async8(ms + 8 * lane, ok ? (const void *)(A.mask + (bit0 >> 5)) : (const void *)A.mask,
+                      ok ? 8 : 0);
+        }
+        if (lane < 16) {
+            const bool ok = myc >= 0;
+            const int64_t o = p_h * A.n_nodes + (ok ? myc : 0);
+            const float *arrs[4] = {A.s0, A.m, A.l, A.c};
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+                cp_async4(cs + a * 64 + 4 * lane, arrs[a] + o, ok ? 4 : 0);
+        }
+    };
+    auto p_advance = [&]() {
+        if (++p_step * 16 >= p_nreal) {
+            p_item += stride;
+            p_load();
+        }
+    };
+
+    p_load();
+#pragma unroll
+    for (int s = 0; s < kGStages - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+        cp_async_commit();
+    }
+
+    int cstage = 0, pstage = kGStages - 1;
+    for (int64_t c_item = (int64_t)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
+        const int64_t part = c_item / A.H;
+        const int64_t h = c_item - part * A.H;
+        const int start = A.rowptr[2 * part];
+        const int e = A.rowptr[2 * part + 1];
+        const int pend = A.rowptr[2 * part + 2];
+        int nreal = e > start ? e - start : 0;
+        if ((start % A.wide) != 0 || (pend % A.wide) != 0 || pend < start + nreal) nreal = 0;
+        const int nsteps = (nreal + 15) >> 4;
+        if (nsteps == 0) continue;
+        const int64_t wrow = (int64_t)A.win[part] * kW;
+        uint32_t bq[C::MT][2];
+#pragma unroll
+        for (int kk = 0; kk < C::MT; ++kk)
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int64_t row = wrow + gid;
+                const int f = 16 * kk + 2 * tig + 8 * u;
+                bq[kk][u] = row < A.n_nodes ? *(const uint32_t *)(Xq + row * A.ldx + h * F + f) : 0u;
+            }
+        float s1r[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t row = wrow + 2 * tig + u;
+            s1r[u] = row < A.n_nodes ? A.s1[h * A.n_nodes + row] : 0.f;
+        }
+        float ds1_acc[2] = {0.f, 0.f};
+        float acc[C::MT][4];
+#pragma unroll
+        for (int j = 0; j < C::MT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+
+        for (int step = 0; step < nsteps; ++step) {
+            cp_async_wait<kGStages - 2>();
+            __syncwarp();
+            const uint32_t xs = sbase + cstage * C::STAGE;
+            const uint32_t *mw = (const uint32_t *)(sgen + cstage * C::STAGE + C::XSTAGE);
+            const float *cv = (const float *)(sgen + cstage * C::STAGE + C::XSTAGE + C::MSTAGE);
+            // dp[c][r] = dout_c . X'_r
+            float dp[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int kk = 0; kk < C::MT; ++kk) {
+                const int q = lane >> 3, rr = lane & 7;
+                const int mrow = (q & 1) * 8 + rr;
+                const int ch = 2 * kk + (q >> 1);
+                const uint32_t ad = mrow * C::XROW + ((ch ^ swz_row<F>(mrow)) << 4);
+                uint32_t a[4];
+                ldsm_x4(xs + ad, a[0], a[1], a[2], a[3]);
+                mma_16816<T>(dp, a, bq[kk][0], bq[kk][1]);
+                if constexpr (SPLIT) {
+                    ldsm_x4(xs + C::TILE + ad, a[0], a[1], a[2], a[3]);
+                    mma_16816<T>(dp, a, bq[kk][0], bq[kk][1]);
+                }
+            }
+            const int c0 = step * 16;
+            float p[4], dz[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int c = gid + 8 * (u >> 1);
+                const int r = 2 * tig + (u & 1);
+                const int bit = (c - c % A.wide) * kW + r * A.wide + c % A.wide;
+                const bool occ = c0 + c < nreal && ((mw[bit >> 5] >> (bit & 31)) & 1u);
+                const float s0c = cv[c], mc = cv[16 + c], lc = cv[32 + c], cc = cv[48 + c];
+                const float z = s0c + s1r[u & 1];
+                const float lr = z > 0.f ? z : A.slope * z;
+                const float pv = occ && lc > 0.f ? __expf(lr - mc) / lc : 0.f;
+                p[u] = pv;
+                dz[u] = pv * (dp[u] - cc) * (z > 0.f ? 1.f : A.slope);
+            }
+            // ds1 (rows): sum over the 16 columns
+            float r0 = dz[0] + dz[2], r1 = dz[1] + dz[3];
+#pragma unroll
+            for (int o = 4; o < 32; o <<= 1) {
+                r0 += __shfl_xor_sync(0xffffffffu, r0, o);
+                r1 += __shfl_xor_sync(0xffffffffu, r1, o);
+            }
+            ds1_acc[0] += r0;
+            ds1_acc[1] += r1;
+            // ds0 (columns): sum over the 8 rows, one atomic per column
+            float c_lo = dz[0] + dz[1], c_hi = dz[2] + dz[3];
+#pragma unroll
+            for (int o = 1; o < 4; o <<= 1) {
+                c_lo += __shfl_xor_sync(0xffffffffu, c_lo, o);
+                c_hi += __shfl_xor_sync(0xffffffffu, c_hi, o);
+            }
+            if (tig == 0) {
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int c = gid + 8 * u;
+                    if (c0 + c < nreal) {
+                        const int ci = A.col[start + c0 + c];
+                        if (ci >= 0 && ci < A.n_nodes)
+                            red_add_f32(A.ds0 + h * A.n_nodes + ci, u ? c_hi : c_lo);
+                    }
+                }
+            }
+            // dX'_r += sum_c p[c][r] dout_c
+            const uint32_t b0 = movmatrix_trans(pack2<T>(p[0], p[1]));
+            const uint32_t b1 = movmatrix_trans(pack2<T>(p[2], p[3]));
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int q = lane >> 3, rr = lane & 7;
+                const int k = (q >> 1) * 8 + rr;
+                const int ch = 2 * j + (q & 1);
+                const uint32_t ad = k * C::XROW + ((ch ^ swz_row<F>(k)) << 4);
+                uint32_t a[4];
+                ldsm_x4_trans(xs + ad, a[0], a[1], a[2], a[3]);
+                mma_16816<T>(acc[j], a, b0, b1);
+                if constexpr (SPLIT) {
+                    ldsm_x4_trans(xs + C::TILE + ad, a[0], a[1], a[2], a[3]);
+                    mma_16816<T>(acc[j], a, b0, b1);
+                }
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                issue(pstage);
+                p_advance();
+            }
+            cp_async_commit();
+            cstage = cstage + 1 == kGStages ? 0 : cstage + 1;
+            pstage = pstage + 1 == kGStages ? 0 : pstage + 1;
+        }
+#pragma unroll
+        for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t row = wrow + 2 * tig + (u & 1);
+                const int f = 16 * j + gid + 8 * (u >> 1);
+                if (row < A.n_nodes) red_add_f32(A.dXp + row * A.ldg + h * F + f, acc[j][u]);
+            }
+        if (gid == 0) {
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int64_t row = wrow + 2 * tig + u;
+                if (row < A.n_nodes) red_add_f32(A.ds1 + h * A.n_nodes + row, ds1_acc[u]);
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+template <typename T, int F, bool SPLIT>
+int run_gat_bwd(const GatBwdArgs &P, cudaStream_t st) {
+    using C = BCfg<T, F, SPLIT>;
+    auto kernel = k_gat_backward<T, F, SPLIT>;
+    static std::once_flag once;
+    static int prep = ATT_OK;
+    std::call_once(once, [&] {
+        prep = cuda_status(
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
+            "cudaFuncSetAttribute");
+    });
+    if (prep != ATT_OK) return prep;
+    const int64_t items = P.n_parts * P.H;
+    if (items == 0) return ATT_OK;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGThreads, C::SMEM);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t want = (items + kGWarps - 1) / kGWarps;
+    const int64_t cap = (int64_t)sm_count() * per_sm;
+    kernel<<<(unsigned)(want < cap ? want : cap), kGThreads, C::SMEM, st>>>(P);
+    return launch_status("k_gat_backward");
+}
+
+template <typename T>
+int dispatch_gat_bwd(const GatBwdArgs &P, cudaStream_t st) {
+    const bool split = P.dout_lo != nullptr;
+    switch (P.F) {
+        case 32: return split ? run_gat_bwd<T, 32, true>(P, st) : run_gat_bwd<T, 32, false>(P, st);
+        case 64: return split ? run_gat_bwd<T, 64, true>(P, st) : run_gat_bwd<T, 64, false>(P, st);
+        case 128: return split ? run_gat_bwd<T, 128, true>(P, st) : run_gat_bwd<T, 128, false>(P, st);
+        default:
+            set_error("fused GAT backward supports F in {32, 64, 128}, got %lld", (long long)P.F);
             return ATT_ERR_UNSUPPORTED;
     }
 }
@@ -567,4 +903,33 @@ extern "C" int att_gat_forward(const int32_t *rowptr, const int32_t *col, const 
         s = launch_status("k_gat_combine");
     }
     return s;
+}
+
+extern "C" int att_gat_backward(const int32_t *rowptr_t, const int32_t *col_t,
+                                const uint32_t *slot_mask_t, const int32_t *window_of_part_t,
+                                int64_t n_parts_t, int window, int wide, const void *Xp,
+                                const void *dout, const void *dout_lo, int x_dtype, int64_t n_nodes, int64_t n_heads,
+                                int64_t F, int64_t ldx, int64_t ldd, const float *s0,
+                                const float *s1, const float *row_max, const float *row_sum,
+                                const float *c, float slope, float *dXp, int64_t ldg, float *ds0,
+                                float *ds1, int32_t *err_flag, void *stream) {
+    clear_error();
+    ATT_CHECK(window == kW, ATT_ERR_UNSUPPORTED, "fused GAT backward needs 8-row windows");
+    ATT_CHECK(wide == 4 || wide == 8 || wide == 16, ATT_ERR_UNSUPPORTED, "wide must be 4, 8 or 16");
+    ATT_CHECK(x_dtype == ATT_F16 || x_dtype == ATT_BF16, ATT_ERR_UNSUPPORTED,
+              "fused GAT backward takes fp16 or bf16 X' and dout");
+    ATT_CHECK(n_heads > 0 && F > 0, ATT_ERR_INVALID, "bad heads / features");
+    ATT_CHECK(ldx % 8 == 0 && ldd % 8 == 0 && ((uintptr_t)Xp & 15) == 0 &&
+                  ((uintptr_t)dout & 15) == 0 && ((uintptr_t)dout_lo & 15) == 0,
+              ATT_ERR_UNSUPPORTED, "X' and dout rows must be 16-byte aligned");
+    ATT_CHECK(s0 && s1 && row_max && row_sum && c && dXp && ds0 && ds1, ATT_ERR_INVALID,
+              "null pointer");
+    if (n_parts_t == 0 || n_nodes == 0) return ATT_OK;
+    ATT_CHECK(rowptr_t && col_t && slot_mask_t && window_of_part_t, ATT_ERR_INVALID,
+              "null format pointer");
+    GatBwdArgs P{rowptr_t, col_t, window_of_part_t, slot_mask_t, n_parts_t, wide, Xp, dout,
+                 dout_lo, n_nodes, n_heads, F, ldx, ldd, s0, s1, row_max, row_sum, c, slope, dXp, ldg,
+                 ds0, ds1, err_flag};
+    cudaStream_t st = (cudaStream_t)stream;
+    return x_dtype == ATT_F16 ? dispatch_gat_bwd<__half>(P, st) : dispatch_gat_bwd<__nv_bfloat16>(P, st);
 }

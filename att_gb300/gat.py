@@ -40,6 +40,55 @@ class GATGraph:
         _lib.call("att_slot_mask", _p(f.edge_slot), f.nnz, _p(self.mask), (n_slots + 31) // 32,
                   _stream())
         self._plan(parts_per_chunk)
+        self._transposed = None
+        self._csr = (rowptr, torch.as_tensor(col))
+
+    def transposed(self):
+        """The graph of the reversed edges (for the backward pass); the graph
+        itself when the CSR is symmetric."""
+        if self._transposed is None:
+            rowptr, col = self._csr
+            rowptr = rowptr.to("cuda").long()
+            col = col.to("cuda").long()
+            n = self.n_nodes
+            rows = torch.repeat_interleave(torch.arange(n, device="cuda"),
+                                           rowptr[1:n + 1] - rowptr[:n])
+            key_t = torch.sort(col * n + rows).values
+            if torch.equal(key_t, rows * n + col):
+                self._transposed = self
+            else:
+                rt, ct = key_t // n, key_t % n
+                rp_t = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+                rp_t[1:] = torch.cumsum(torch.bincount(rt, minlength=n), 0)
+                self._transposed = GATGraph(rp_t.to(torch.int32), ct.to(torch.int32),
+                                            window=self.window, wide=self.wide)
+        return self._transposed
+
+    def attention_backward(self, Xp, dout, s0, s1, row_max, row_sum, c, n_heads, slope=0.2):
+        """Fused backward of attention(mode=MODE_ADD): returns (dXp_agg fp32
+        [n_nodes, H*F], ds0, ds1 fp32 [H, n_nodes]) with
+        dXp_agg[j] = sum_i p_ij dout_i and ds0 / ds1 the gradients of the
+        scores s0 / s1.  ``c[h][i] = dout_i . out_i``."""
+        require_cuda()
+        T = self.transposed()
+        f = T.fmt
+        N = self.n_nodes
+        F = Xp.shape[1] // n_heads
+        Xp = Xp.contiguous()
+        dout32 = dout.float()
+        dout = dout32.to(Xp.dtype).contiguous()
+        dout_lo = (dout32 - dout.float()).to(Xp.dtype).contiguous()
+        dXp = torch.zeros(N, n_heads * F, dtype=torch.float32, device=Xp.device)
+        ds0 = torch.zeros(n_heads, N, dtype=torch.float32, device=Xp.device)
+        ds1 = torch.zeros(n_heads, N, dtype=torch.float32, device=Xp.device)
+        _lib.call("att_gat_backward", _p(f.rowptr), _p(f.col), _p(T.mask), _p(f.window_of_part),
+                  f.n_parts, self.window, self.wide, _p(Xp), _p(dout), _p(dout_lo),
+                  _DT[Xp.dtype], N, n_heads,
+                  F, Xp.stride(0), dout.stride(0), _p(s0.contiguous()), _p(s1.contiguous()),
+                  _p(row_max.contiguous()), _p(row_sum.contiguous()), _p(c.contiguous()),
+                  float(slope), _p(dXp), dXp.stride(0), _p(ds0), _p(ds1), None, _stream())
+        return dXp, ds0, ds1
+
 
     def _plan(self, T):
         win = self.fmt.window_of_part.long()
@@ -106,3 +155,64 @@ class GATGraph:
                   _DT[Xp.dtype], N, n_heads, F, Xp.stride(0), mode, _p(s0), _p(s1), float(slope),
                   _p(out), out.stride(0), _p(rmax), _p(rsum), _p(partial), None, _stream())
         return out, rmax, rsum
+
+
+class GATAttention(torch.autograd.Function):
+    """Additive multi-head GAT aggregation with the fused forward and backward
+    kernels: out_i = sum_j softmax_j(LeakyReLU(X'_i.a0 + X'_j.a1)) X'_j per
+    head (end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198 without dropout).
+    Xp [N, H*F] fp16/bf16, a0/a1 [H, F]; returns fp32 [N, H*F]."""
+
+    @staticmethod
+    def forward(ctx, Xp, a0, a1, graph, n_heads, slope):
+        from . import gat_ops
+        N = graph.n_nodes
+        F = Xp.shape[1] // n_heads
+        X3 = Xp.view(N, n_heads, F).permute(1, 0, 2)
+        # attention vectors stay fp32: rounding them would shift every score
+        s0 = gat_ops.node_scores(X3, a0.float())
+        s1 = gat_ops.node_scores(X3, a1.float())
+        out, rmax, rsum = graph.attention(Xp, n_heads=n_heads, mode=MODE_ADD, s0=s0, s1=s1,
+                                          slope=slope)
+        ctx.save_for_backward(Xp, a0, a1, s0, s1, rmax, rsum, out)
+        ctx.graph, ctx.n_heads, ctx.slope = graph, n_heads, slope
+        return out
+
+    @staticmethod
+    def backward(ctx, dout):
+        Xp, a0, a1, s0, s1, rmax, rsum, out = ctx.saved_tensors
+        G, H, slope = ctx.graph, ctx.n_heads, ctx.slope
+        N = G.n_nodes
+        F = Xp.shape[1] // H
+        dout = dout.contiguous()
+        c = (dout.view(N, H, F) * out.view(N, H, F)).sum(-1).t().contiguous()
+        dXp, ds0, ds1 = G.attention_backward(Xp, dout, s0, s1, rmax, rsum, c, H, slope)
+        X3 = Xp.view(N, H, F).float()
+        dX3 = dXp.view(N, H, F) + ds0.t()[:, :, None] * a0.float()[None] + \
+            ds1.t()[:, :, None] * a1.float()[None]
+        da0 = torch.einsum("hn,nhf->hf", ds0, X3).to(a0.dtype)
+        da1 = torch.einsum("hn,nhf->hf", ds1, X3).to(a1.dtype)
+        return dX3.reshape(N, H * F).to(Xp.dtype), da0, da1, None, None, None
+
+
+class GATConv(torch.nn.Module):
+    """Multi-head GAT layer on the fused kernels: X -> X W (per head F
+    features) -> additive attention -> [N, H*F] fp32 (concatenated heads).
+    Parameters as the reference's GATConv_multi
+    (end2end_head/gat_final/mgat_csr/mgat_conv.py:154-198): W Xavier-normal,
+    a0 / a1 [H, F]."""
+
+    def __init__(self, in_dim, out_dim, heads=1, slope=0.2, dtype=torch.bfloat16):
+        super().__init__()
+        gain = torch.nn.init.calculate_gain("relu")
+        self.W = torch.nn.Parameter(torch.empty(in_dim, heads * out_dim))
+        torch.nn.init.xavier_normal_(self.W, gain=gain)
+        self.a0 = torch.nn.Parameter(torch.empty(heads, out_dim))
+        self.a1 = torch.nn.Parameter(torch.empty(heads, out_dim))
+        torch.nn.init.xavier_normal_(self.a0, gain=gain)
+        torch.nn.init.xavier_normal_(self.a1, gain=gain)
+        self.heads, self.out_dim, self.slope, self.dtype = heads, out_dim, slope, dtype
+
+    def forward(self, X, graph):
+        Xp = torch.mm(X.to(self.dtype), self.W.to(self.dtype))
+        return GATAttention.apply(Xp, self.a0, self.a1, graph, self.heads, self.slope)

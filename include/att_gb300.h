@@ -265,7 +265,10 @@ ATT_API int att_slot_mask(const int32_t *edge_slot, int64_t nnz, uint32_t *mask,
  * `partial` ([n_slots][n_heads][8][F+2] fp32 scratch); multi_chunk_begin holds
  * (first, end) chunk pairs of the n_multi windows spread over several chunks.
  * row_max / row_sum ([n_heads][n_nodes], may be NULL) receive the softmax
- * statistics for the backward pass.  8-row windows, F in {32, 64, 128},
+ * statistics for the backward pass; when row_sum is given the aggregation
+ * also runs with the probabilities split into a hi + lo pair of 16-bit
+ * values, so the output is fp32-consistent with them (the backward relies on
+ * dout . out matching its recomputed probabilities).  8-row windows, F in {32, 64, 128},
  * fp16 or bf16 X'.  Every row < n_nodes of out is written. */
 ATT_API int att_gat_forward(const int32_t *rowptr, const int32_t *col, const uint32_t *slot_mask,
                    const int32_t *window_of_part, int64_t n_parts,
@@ -275,6 +278,26 @@ ATT_API int att_gat_forward(const int32_t *rowptr, const int32_t *col, const uin
                    int64_t ldx, int mode, const float *s0, const float *s1, float slope,
                    float *out, int64_t ldo, float *row_max, float *row_sum, float *partial,
                    int32_t *err_flag, void *stream);
+
+/* Backward of the additive GAT layer (mode 1 of att_gat_forward), fused: with
+ * the forward's row max / sum and c[h][i] = dout_i . out_i,
+ *   p_ij = exp(LeakyReLU(s0_i + s1_j) - m_i) / l_i,
+ *   dz_ij = p_ij (dout_i . X'_j - c_i) LeakyReLU'(s0_i + s1_j),
+ *   dXp[j] += p_ij dout_i  (SpMM adjoint),  ds1[j] += dz_ij,  ds0[i] += dz_ij,
+ * in one pass over the block format of the TRANSPOSED graph (for a symmetric
+ * graph, the forward format itself).  dXp, ds0, ds1 are accumulated
+ * (red.add): zero them first.  dout_lo (may be NULL) is dout minus its
+ * rounding to the 16-bit type: with it both products run as a hi + lo pair,
+ * which keeps bf16 gradients at fp16-like accuracy.  Replaces the backward of
+ * end2end_ori/gat_final/mgat_csr/mgat_conv.py:34-151 (two rowsum SpMMs, an
+ * SDDMM, a broadcast and a transposed SpMM). */
+ATT_API int att_gat_backward(const int32_t *rowptr_t, const int32_t *col_t,
+                   const uint32_t *slot_mask_t, const int32_t *window_of_part_t,
+                   int64_t n_parts_t, int window, int wide, const void *Xp, const void *dout,
+                   const void *dout_lo, int x_dtype, int64_t n_nodes, int64_t n_heads, int64_t F, int64_t ldx,
+                   int64_t ldd, const float *s0, const float *s1, const float *row_max,
+                   const float *row_sum, const float *c, float slope, float *dXp, int64_t ldg,
+                   float *ds0, float *ds1, int32_t *err_flag, void *stream);
 
 #ifdef __cplusplus
 }

@@ -346,3 +346,27 @@ def gat_dot_layer_cpu_fp32(rowptr, col, Xp, slope=0.2):
     l = torch.zeros(n).index_add_(0, rows, p)
     out = torch.zeros(n, Xp.shape[1]).index_add_(0, rows, p[:, None] * Xc)
     return out / l.clamp_min(1e-30)[:, None]
+
+
+def gat_add_layer_torch(rowptr, col, Xp, a0, a1, slope=0.2):
+    """Differentiable torch restatement (use fp64 tensors) of the additive
+    multi-head GAT aggregation (end2end_ori/gat_final/mgat_csr/mgat_conv.py:
+    173-198 without dropout): Xp [N, H*F], a0/a1 [H, F] -> [N, H*F].
+    Its autograd gradient is the reference gradient of the backward tests."""
+    import torch
+    rowptr = torch.as_tensor(rowptr).long()
+    col = torch.as_tensor(col).long()
+    H, F = a0.shape
+    N = rowptr.numel() - 1
+    X3 = Xp.view(-1, H, F)[:N]
+    s0 = (X3 * a0[None]).sum(-1)
+    s1 = (X3 * a1[None]).sum(-1)
+    rows = torch.repeat_interleave(torch.arange(N), rowptr[1:] - rowptr[:-1])
+    e = torch.nn.functional.leaky_relu(s0[rows] + s1[col], slope)
+    m = torch.full((N, H), float("-inf"), dtype=e.dtype).scatter_reduce(
+        0, rows[:, None].expand(-1, H), e, "amax").detach()
+    ex = torch.exp(e - m[rows])
+    l = torch.zeros(N, H, dtype=e.dtype).index_add(0, rows, ex)
+    p = ex / l[rows]
+    out = torch.zeros(N, H, F, dtype=e.dtype).index_add(0, rows, p[:, :, None] * X3[col])
+    return out.reshape(N, H * F)
