@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     int64_t p_item = (int64_t)blockIdx.x * kGWarps + warp;
     int64_t p_h = 0;
     int p_part = 0, p_part_end = 0, p_start = 0, p_nreal = 0, p_pend = 0, p_step = 0;
+    int p_myc = -1;  // column ids of the producer's position, fetched one step ahead
     auto p_set_part = [&]() {  // returns with p_part < p_part_end and a non-empty part, or exhausted
         while (true) {
             while (p_part < p_part_end) {
@@ -168,8 +169,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
         const uint32_t ms = xs + C::XSTAGE;
         const uint32_t ss = ms + C::MSTAGE;
         const int c0 = p_step * 16;
-        int myc = -1;
-        if (c0 + (lane & 15) < p_nreal) myc = A.col[p_start + c0 + (lane & 15)];
+        int myc = p_myc;
         if (myc >= A.n_nodes || myc < -1) {
             if (A.err) atomicOr(A.err, 1);
             myc = -1;
@@ -205,14 +205,21 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             (void)ss;
         }
     };
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_nreal)
+            p_myc = A.col[p_start + p_step * 16 + (lane & 15)];
+    };
     auto p_advance = [&]() {
         if (++p_step * 16 >= p_nreal) {
             ++p_part;
             p_set_part();
         }
+        p_fetch();
     };
 
     p_begin();
+    p_fetch();
 #pragma unroll
     for (int s = 0; s < kGStages - 1; ++s) {
         if (p_item < n_items) {
@@ -584,7 +591,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
 
     int64_t p_item = (int64_t)blockIdx.x * kGWarps + warp;
     int64_t p_h = 0;
-    int p_start = 0, p_nreal = 0, p_pend = 0, p_step = 0;
+    int p_start = 0, p_nreal = 0, p_pend = 0, p_step = 0, p_myc = -1;
     auto p_load = [&]() {
         while (p_item < n_items) {
             const int64_t part = p_item / A.H;
@@ -607,8 +614,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         const uint32_t ms = xs + C::XSTAGE;
         const uint32_t cs = ms + C::MSTAGE;
         const int c0 = p_step * 16;
-        int myc = -1;
-        if (c0 + (lane & 15) < p_nreal) myc = A.col[p_start + c0 + (lane & 15)];
+        int myc = p_myc;  // fetched one step ahead
         if (myc >= A.n_nodes || myc < -1) {
             if (A.err) atomicOr(A.err, 1);
             myc = -1;
@@ -641,14 +647,21 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
                 cp_async4(cs + a * 64 + 4 * lane, arrs[a] + o, ok ? 4 : 0);
         }
     };
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_nreal)
+            p_myc = A.col[p_start + p_step * 16 + (lane & 15)];
+    };
     auto p_advance = [&]() {
         if (++p_step * 16 >= p_nreal) {
             p_item += stride;
             p_load();
         }
+        p_fetch();
     };
 
     p_load();
+    p_fetch();
 #pragma unroll
     for (int s = 0; s < kGStages - 1; ++s) {
         if (p_item < n_items) {

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
 
     // ---- producer cursor ----
     int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
-    int p_step = 0;
+    int p_step = 0, p_myc = -1;
     PartInfo p_pi = {0, 0, 0};
     int p_fc = 0;
     auto p_load = [&]() {
@@ -123,8 +123,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
         const uint32_t xs = sbase + stage * C::STAGE;
         const uint32_t vs = xs + C::XSTAGE;
         const int c0 = p_step * 16;
-        int myc = -1;
-        if (c0 + (lane & 15) < p_pi.nreal) myc = __ldg(col + p_pi.start + c0 + (lane & 15));
+        int myc = p_myc;  // loaded one step ahead
         const int64_t fbase = (int64_t)p_fc * FC;
 #pragma unroll
         for (int i = 0; i < 16 / C::RPP; ++i) {
@@ -149,14 +148,23 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
             cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
         }
     };
+    // column ids of the producer's position, fetched one step ahead so the
+    // load latency overlaps the consumer's work instead of stalling issue()
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
+            p_myc = __ldg(col + p_pi.start + p_step * 16 + (lane & 15));
+    };
     auto p_advance = [&]() {
         if (++p_step >= p_pi.nsteps) {
             p_item += stride;
             p_load();
         }
+        p_fetch();
     };
 
     p_load();
+    p_fetch();
 #pragma unroll
     for (int s = 0; s < kStages - 1; ++s) {
         if (p_item < n_items) {
@@ -314,7 +322,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm16_tma(
     __syncwarp();
 
     int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
-    int p_step = 0, p_fc = 0, p_pend = 0;
+    int p_step = 0, p_fc = 0, p_pend = 0, p_myc = -1;
     PartInfo p_pi = {0, 0, 0};
     auto p_load = [&]() {
         while (p_item < n_items) {
@@ -333,19 +341,19 @@ __global__ void __launch_bounds__(kThreads) k_spmm16_tma(
         const int vcols = min(16, p_pend - p_pi.start - c0);
         const uint32_t vbytes = (uint32_t)(vcols * W * 2);
         if (lane == 0) mbar_arrive_expect_tx(bar, C::FCH * 4 * 4 * kPitch + vbytes);
+        int y[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {  // ids of rows 4*lane+i (prefetched one step ahead)
+            int cidx = __shfl_sync(0xffffffffu, p_myc, (4 * lane + i) & 15);
+            if (cidx >= n_x || cidx < -1) {
+                if (err && lane < 4) atomicOr(err, 1);
+                cidx = -1;
+            }
+            y[i] = cidx >= 0 ? cidx : oob_row;
+        }
+        (void)c0;
         __syncwarp();
         if (lane < 4) {
-            int y[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int c = c0 + 4 * lane + i;
-                int cidx = c < p_pi.nreal ? __ldg(col + p_pi.start + c) : -1;
-                if (cidx >= n_x || cidx < -1) {
-                    if (err) atomicOr(err, 1);
-                    cidx = -1;
-                }
-                y[i] = cidx >= 0 ? cidx : oob_row;
-            }
 #pragma unroll
             for (int ch = 0; ch < C::FCH; ++ch) {
                 const int64_t fb = (int64_t)p_fc * FC + 64 * ch;
@@ -357,14 +365,23 @@ __global__ void __launch_bounds__(kThreads) k_spmm16_tma(
             bulk_g2s(vtile(stage), val + (int64_t)(p_pi.start + c0) * W, vbytes, bar);
         }
     };
+    // column ids of the producer's position, fetched one step ahead so the
+    // load latency overlaps the consumer's work instead of stalling issue()
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
+            p_myc = __ldg(col + p_pi.start + p_step * 16 + (lane & 15));
+    };
     auto p_advance = [&]() {
         if (++p_step >= p_pi.nsteps) {
             p_item += stride;
             p_load();
         }
+        p_fetch();
     };
 
     p_load();
+    p_fetch();
     int inflight = 0;
 #pragma unroll
     for (int s = 0; s < S - 1; ++s) {
@@ -503,7 +520,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
     const int gid = lane >> 2, tig = lane & 3;
 
     int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
-    int p_step = 0, p_fc = 0;
+    int p_step = 0, p_fc = 0, p_myc = -1;
     PartInfo p_pi = {0, 0, 0};
     auto p_load = [&]() {
         while (p_item < n_items) {
@@ -519,8 +536,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
         const uint32_t xs = sbase + stage * C::STAGE;
         const uint32_t vs = xs + C::XSTAGE;
         const int c0 = p_step * 16;
-        int myc = -1;
-        if (c0 + (lane & 15) < p_pi.nreal) myc = __ldg(col + p_pi.start + c0 + (lane & 15));
+        int myc = p_myc;  // loaded one step ahead
         const int64_t fbase = (int64_t)p_fc * FC;
 #pragma unroll
         for (int i = 0; i < 16 / C::RPP; ++i) {
@@ -545,14 +561,23 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
             cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
         }
     };
+    // column ids of the producer's position, fetched one step ahead so the
+    // load latency overlaps the consumer's work instead of stalling issue()
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
+            p_myc = __ldg(col + p_pi.start + p_step * 16 + (lane & 15));
+    };
     auto p_advance = [&]() {
         if (++p_step >= p_pi.nsteps) {
             p_item += stride;
             p_load();
         }
+        p_fetch();
     };
 
     p_load();
+    p_fetch();
 #pragma unroll
     for (int s = 0; s < kStages - 1; ++s) {
         if (p_item < n_items) {
@@ -618,6 +643,237 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
             cp_async_commit();
             cstage = cstage + 1 == kStages ? 0 : cstage + 1;
             pstage = pstage + 1 == kStages ? 0 : pstage + 1;
+        }
+        const int wrow = __ldg(win + part);
+        const bool add = __ldg(atomic + part) != 0;
+        const int64_t f0 = (int64_t)fc * FC;
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) {
+            const int64_t r0 = (int64_t)wrow * W + t * 8 + 2 * tig;
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int64_t fa = f0 + 16 * j + gid;
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int64_t r = r0 + (h & 1);
+                    const int64_t f = fa + (h >> 1) * 8;
+                    if (r >= 0 && r < m_out && f < F) {
+                        float *dst = Y + r * ldy + f;
+                        if (add) red_add_f32(dst, acc[j][t][h]);
+                        else *dst = acc[j][t][h];
+                    }
+                    acc[j][t][h] = 0.f;
+                }
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// FP8 E4M3 features with per-row fp32 scales (values fp16)
+// ---------------------------------------------------------------------------
+// The gathered rows are e4m3 (half the bytes of fp16), staged by 16-byte
+// cp.async in a deep ring; the consumer dequantizes the step's 16 rows into
+// one fp16 tile per warp -- cvt e4m3x2 -> f16x2 is exact, then one multiply by
+// the row's scale (done here on X, where it cannot underflow to fp16
+// subnormals as it could on the small block values) -- and runs the fp16
+// ldmatrix.trans + mma.sync path with fp32 accumulation.
+constexpr int kF8Stages = 8;
+
+template <int W, int FC>
+struct CfgF8 {
+    static constexpr int XROW8 = FC;             // bytes per gathered e4m3 row
+    static constexpr int XSTAGE = 16 * XROW8;
+    static constexpr int VSTAGE = 16 * W * 2;
+    static constexpr int SSTAGE = 64;            // 16 fp32 scales
+    static constexpr int STAGE = XSTAGE + VSTAGE + SSTAGE;
+    static constexpr int XROW16 = FC * 2;        // dequantized fp16 tile row
+    static constexpr int TILE16 = 16 * XROW16;
+    static constexpr int WARP_SMEM = kF8Stages * STAGE + TILE16;
+    static constexpr int SMEM = kWarps * WARP_SMEM;
+    static constexpr int CPR = FC / 16;          // 16-byte e4m3 chunks per row
+    static constexpr int MT = FC / 16;
+    static constexpr int NT = W / 8;
+    static constexpr int VCH = VSTAGE / 16;
+};
+
+__device__ __forceinline__ uint32_t e4m3x2_to_f16x2(uint16_t v) {
+    uint32_t r;
+    asm("cvt.rn.f16x2.e4m3x2 %0, %1;\n" : "=r"(r) : "h"(v));
+    return r;
+}
+
+template <int W, int FC, int WIDE>
+__global__ void __launch_bounds__(kThreads) k_spmm_fp8(
+    const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+    const __half *__restrict__ val, const int32_t *__restrict__ win,
+    const int32_t *__restrict__ atomic, int64_t n_parts, const uint8_t *__restrict__ X,
+    const float *__restrict__ xscale, int64_t n_x, int64_t F, int64_t ldx, float *__restrict__ Y,
+    int64_t m_out, int64_t ldy, int n_chunks, int32_t *__restrict__ err) {
+    using C = CfgF8<W, FC>;
+    constexpr int S = kF8Stages;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
+    const unsigned char *sgen = smem + warp * C::WARP_SMEM;
+    const uint32_t tile = sbase + S * C::STAGE;
+    const int64_t n_items = n_parts * n_chunks;
+    const int64_t stride = (int64_t)gridDim.x * kWarps;
+    const int gid = lane >> 2, tig = lane & 3;
+
+    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    int p_step = 0, p_fc = 0, p_myc = -1;
+    PartInfo p_pi = {0, 0, 0};
+    auto p_load = [&]() {
+        while (p_item < n_items) {
+            int64_t part = p_item / n_chunks;
+            p_fc = (int)(p_item - part * n_chunks);
+            p_pi = part_info<WIDE>(rowptr, part, err);
+            p_step = 0;
+            if (p_pi.nsteps > 0) return;
+            p_item += stride;
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * C::STAGE;
+        const uint32_t vs = xs + C::XSTAGE;
+        const uint32_t ss = vs + C::VSTAGE;
+        const int c0 = p_step * 16;
+        int myc = p_myc;  // loaded one step ahead
+        if (myc >= n_x || myc < -1) {
+            if (err) atomicOr(err, 1);
+            myc = -1;
+        }
+        const int64_t fbase = (int64_t)p_fc * FC;
+#pragma unroll
+        for (int i = 0; i < 16 * C::CPR / 32; ++i) {
+            const int idx = i * 32 + lane;
+            const int r = idx / C::CPR, ch = idx % C::CPR;
+            const int cidx = __shfl_sync(0xffffffffu, myc, r);
+            const int64_t f = fbase + ch * 16;
+            const bool ok = cidx >= 0 && f < F;
+            cp_async16(xs + r * C::XROW8 + ch * 16, ok ? X + (int64_t)cidx * ldx + f : X, ok ? 16 : 0);
+        }
+#pragma unroll
+        for (int q = lane; q < C::VCH; q += 32) {
+            const int e = q * 8;
+            const int blk = e / (W * WIDE);
+            const bool ok = c0 + blk * WIDE < p_pi.nreal;
+            const __half *src = val + ((int64_t)(p_pi.start + c0) * W + e);
+            cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
+        }
+        if (lane < 16) {
+            const bool ok = myc >= 0;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(ss + 4 * lane),
+                         "l"(ok ? xscale + myc : xscale), "r"(ok ? 4 : 0));
+        }
+    };
+    // column ids of the producer's position, fetched one step ahead so the
+    // load latency overlaps the consumer's work instead of stalling issue()
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
+            p_myc = __ldg(col + p_pi.start + p_step * 16 + (lane & 15));
+    };
+    auto p_advance = [&]() {
+        if (++p_step >= p_pi.nsteps) {
+            p_item += stride;
+            p_load();
+        }
+        p_fetch();
+    };
+
+    p_load();
+    p_fetch();
+#pragma unroll
+    for (int s = 0; s < S - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+        cp_async_commit();
+    }
+
+    float acc[C::MT][C::NT][4];
+#pragma unroll
+    for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
+
+    int cstage = 0, pstage = S - 1;
+    for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const int64_t part = c_item / n_chunks;
+        const int fc = (int)(c_item - part * n_chunks);
+        const PartInfo pi = part_info<WIDE>(rowptr, part, nullptr);
+        for (int step = 0; step < pi.nsteps; ++step) {
+            cp_async_wait<S - 2>();
+            __syncwarp();
+            const unsigned char *x8 = sgen + cstage * C::STAGE;
+            const float *sc = (const float *)(x8 + C::XSTAGE + C::VSTAGE);
+            const uint32_t vs = sbase + cstage * C::STAGE + C::XSTAGE;
+            // dequantize: 8 lanes per row, one 16-byte e4m3 chunk each
+#pragma unroll
+            for (int i = 0; i < 16 * C::CPR / 32; ++i) {
+                const int idx = i * 32 + lane;
+                const int r = idx / C::CPR, ch = idx % C::CPR;
+                const uint4 raw = *reinterpret_cast<const uint4 *>(x8 + r * C::XROW8 + ch * 16);
+                const __half2 s2 = __float2half2_rn(sc[r]);
+                const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
+                uint32_t h[8];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    uint32_t lo = e4m3x2_to_f16x2((uint16_t)(w[k] & 0xffffu));
+                    uint32_t hi = e4m3x2_to_f16x2((uint16_t)(w[k] >> 16));
+                    __half2 l2 = __hmul2(*reinterpret_cast<__half2 *>(&lo), s2);
+                    __half2 h2 = __hmul2(*reinterpret_cast<__half2 *>(&hi), s2);
+                    h[2 * k] = *reinterpret_cast<uint32_t *>(&l2);
+                    h[2 * k + 1] = *reinterpret_cast<uint32_t *>(&h2);
+                }
+                // fp16 chunks 2ch, 2ch+1 of row r, XOR-swizzled as in k_spmm16
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int c16 = 2 * ch + u;
+                    const uint32_t dst = tile + r * C::XROW16 + ((c16 ^ swz<C::XROW16>(r)) << 4);
+                    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};\n" ::"r"(dst),
+                                 "r"(h[4 * u]), "r"(h[4 * u + 1]), "r"(h[4 * u + 2]),
+                                 "r"(h[4 * u + 3])
+                                 : "memory");
+                }
+            }
+            __syncwarp();
+            uint32_t b[C::NT][2];
+            {
+                const int q = lane >> 3, rr = lane & 7;
+                if constexpr (C::NT == 2) {
+                    const int kb = q & 1, r = (q >> 1) * 8 + rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x4(vs + e * 2, b[0][0], b[0][1], b[1][0], b[1][1]);
+                } else {
+                    const int kb = q & 1, r = rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x2(vs + e * 2, b[0][0], b[0][1]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int q = lane >> 3, rr = lane & 7;
+                const int k = (q >> 1) * 8 + rr;
+                const int ch = 2 * j + (q & 1);
+                uint32_t a[4];
+                ldsm_x4_trans(tile + k * C::XROW16 + ((ch ^ swz<C::XROW16>(k)) << 4), a[0], a[1],
+                              a[2], a[3]);
+#pragma unroll
+                for (int t = 0; t < C::NT; ++t) mma_16816<__half>(acc[j][t], a, b[t][0], b[t][1]);
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                issue(pstage);
+                p_advance();
+            }
+            cp_async_commit();
+            cstage = cstage + 1 == S ? 0 : cstage + 1;
+            pstage = pstage + 1 == S ? 0 : pstage + 1;
         }
         const int wrow = __ldg(win + part);
         const bool add = __ldg(atomic + part) != 0;
@@ -775,6 +1031,27 @@ constexpr int kTmaStages = 5;
 // att_set_option("spmm_gather", ...).
 int g_spmm_gather = 0;
 
+template <int W, int FC, int WIDE>
+int launch_fp8(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+               const int32_t *atomic, int64_t n_parts, const void *X, const float *xscale,
+               int64_t n_x, int64_t F, int64_t ldx, float *Y, int64_t m_out, int64_t ldy,
+               int32_t *err, cudaStream_t st) {
+    using C = CfgF8<W, FC>;
+    auto kernel = k_spmm_fp8<W, FC, WIDE>;
+    static std::once_flag once;
+    static int prep = ATT_OK;
+    std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+    if (prep != ATT_OK) return prep;
+    const int n_chunks = (int)((F + FC - 1) / FC);
+    const int64_t items = n_parts * n_chunks;
+    if (items == 0) return ATT_OK;
+    const int grid = occupancy_grid(kernel, C::SMEM, items);
+    kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const __half *)val, win, atomic,
+                                            n_parts, (const uint8_t *)X, xscale, n_x, F, ldx, Y,
+                                            m_out, ldy, n_chunks, err);
+    return launch_status("k_spmm_fp8");
+}
+
 template <typename T, int W, int WIDE>
 int dispatch_fc16(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
                   const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
@@ -886,7 +1163,26 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
         return dispatch_fc32<16, 8>(rowptr, col, val, window_of_part, atomic, n_parts, X, n_x_rows,
                                     F, ldx, Y, m_out, ldy, err_flag, st);
     }
-    (void)x_scale;
+    if (val_dtype == ATT_F16 && x_dtype == ATT_F8E4M3) {
+        ATT_CHECK(x_scale != nullptr, ATT_ERR_INVALID, "fp8 features need per-row scales");
+        ATT_CHECK(wide == 8 || wide == 16, ATT_ERR_UNSUPPORTED, "fp16 values need wide 8 or 16");
+        ATT_CHECK(F % 16 == 0 && ldx % 16 == 0 && ((uintptr_t)X & 15) == 0 &&
+                      ((uintptr_t)val & 15) == 0 && ldx >= F,
+                  ATT_ERR_UNSUPPORTED,
+                  "fp8 SpMM needs F and ldx multiples of 16 and 16-byte aligned X and values");
+#define ATT_F8(Wv, FCv, WIDEv)                                                                \
+    return launch_fp8<Wv, FCv, WIDEv>(rowptr, col, val, window_of_part, atomic, n_parts, X,   \
+                                      x_scale, n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st)
+        if (F <= 64) {
+            if (window == 8) { if (wide == 8) ATT_F8(8, 64, 8); ATT_F8(8, 64, 16); }
+            if (wide == 8) ATT_F8(16, 64, 8);
+            ATT_F8(16, 64, 16);
+        }
+        if (window == 8) { if (wide == 8) ATT_F8(8, 128, 8); ATT_F8(8, 128, 16); }
+        if (wide == 8) ATT_F8(16, 128, 8);
+        ATT_F8(16, 128, 16);
+#undef ATT_F8
+    }
     set_error("unsupported (val_dtype=%d, x_dtype=%d) combination", val_dtype, x_dtype);
     return ATT_ERR_UNSUPPORTED;
 }

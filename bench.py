@@ -131,6 +131,7 @@ class SpmmProducts:
     N, MEAN_DEG, GAMMA, SEED, F, F_REAL = 2_449_029, 25, 2.2, 2, 128, 100
 
     e2e_api = "SpMM_sr_bcrs.forward_fp16_gnn"
+    x_kind = "fp16"
 
     def __init__(self, device, scale=1.0, light=False):
         import torch
@@ -161,7 +162,21 @@ class SpmmProducts:
         real = (f.rowptr[1::2] - f.rowptr[0:-1:2]).sum().item()
         self.U = int(real)  # distinct (8-row window, column) pairs = gathered X rows
         F = self.F
-        self.bytes_alg = 4 * (n + 1) + self.nnz * (4 + 2) + self.U * F * 2 + n * F * 4
+        self.val = f.val
+        self.x_scale = None
+        self.Xk = self.X
+        sx = 2
+        self.Xf64 = X.double()  # unquantized features (for the error report)
+        if self.x_kind == "bf16":
+            self.val = f.val.to(torch.bfloat16)
+            self.Xk = X.to(torch.bfloat16)
+        elif self.x_kind == "fp8":
+            amax = X.abs().amax(1).clamp_min(1e-12)
+            self.x_scale = (amax / 448.0).float().contiguous()
+            self.Xk = (X / self.x_scale[:, None]).to(torch.float8_e4m3fn)
+            sx = 1
+        self.bytes_alg = (4 * (n + 1) + self.nnz * (4 + 2) + self.U * F * sx + n * F * 4
+                          + (self.U * 4 if self.x_kind == "fp8" else 0))
         self.flops = 2 * self.nnz * F
         self.launches_per_step = 2  # k_zero_uncovered + k_spmm16
         self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz,
@@ -169,29 +184,35 @@ class SpmmProducts:
                        "mean_degree": self.MEAN_DEG, "seed": self.SEED,
                        "format": "window 8, wide 8, partSize 32",
                        "parts": f.n_parts, "condensed_cols": f.n_condensed,
-                       "gathered_rows_U8": self.U, "x_dtype": "fp16", "y_dtype": "fp32",
+                       "gathered_rows_U8": self.U, "x_dtype": self.x_kind, "y_dtype": "fp32",
                        "l2": "inputs larger than L2 (no flush)"}
 
     def step(self):
         from att_gb300 import ops
         f = self.fmt
-        ops.spmm(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, self.X, self.n, out=self.Y)
+        ops.spmm(f.rowptr, f.col, self.val, f.window_of_part, f.atomic, self.Xk, self.n,
+                 out=self.Y, x_scale=self.x_scale)
 
     # end to end through the reference-facing drop-in, host buffers
     def e2e_setup(self):
         torch = self.torch
-        self.Xh = self.X.cpu().pin_memory()
+        self.Xh = self.Xk.cpu().pin_memory()
         self.Yh = torch.empty(self.n, self.F, dtype=torch.float32).pin_memory()
         from att_gb300.compat import SpMM_sr_bcrs
         self._mod = SpMM_sr_bcrs
-        self.h2d = self.Xh.numel() * 2
+        self.h2d = self.Xh.numel() * self.Xh.element_size()
         self.d2h = self.Yh.numel() * 4
 
     def e2e_step(self):
         f = self.fmt
         Xd = self.Xh.to("cuda", non_blocking=True)
-        Y = self._mod.forward_fp16_gnn(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, Xd,
-                                       self.rowptr.shape[0] - 1, self.F, self.n)[0]
+        if self.x_kind == "fp16":
+            Y = self._mod.forward_fp16_gnn(f.rowptr, f.col, f.val, f.window_of_part, f.atomic,
+                                           Xd, self.rowptr.shape[0] - 1, self.F, self.n)[0]
+        else:
+            from att_gb300 import ops
+            Y = ops.spmm(f.rowptr, f.col, self.val, f.window_of_part, f.atomic, Xd, self.n,
+                         x_scale=self.x_scale)
         self.Yh.copy_(Y, non_blocking=True)
 
     def check(self):
@@ -208,7 +229,31 @@ class SpmmProducts:
         ev = (self.deg[rows].float() * self.deg[self.colidx.long()].float()).half().float()
         rs = torch.zeros(self.rowptr.shape[0] - 1, device=self.X.device).index_add_(0, rows, ev)
         err = ((Y1 - rs[: self.n]).abs().max() / rs.abs().max().clamp_min(1e-30)).item()
+        self.err_vs_fp64 = self.sample_error()
         return err
+
+    def sample_error(self, rows=20000):
+        """Error of this dtype's kernel against the FP64 product on the
+        unquantized features, for the first `rows` rows of the full graph
+        (normwise max and Frobenius relative)."""
+        torch = self.torch
+        from att_gb300 import ops
+        import numpy as np
+        f = self.fmt
+        Y = ops.spmm(f.rowptr, f.col, self.val, f.window_of_part, f.atomic, self.Xk, self.n,
+                     x_scale=self.x_scale)
+        rows = min(rows, self.n)
+        rp = self.rowptr[: rows + 1].long()
+        col = self.colidx[: int(rp[-1])].long()
+        ridx = torch.repeat_interleave(torch.arange(rows, device=rp.device), rp[1:] - rp[:-1])
+        vals = (self.deg[ridx].float() * self.deg[col].float()).half().double()
+        X64 = self.X.double() if self.x_kind == "fp16" else self.Xf64
+        ref = torch.zeros(rows, self.F, dtype=torch.float64, device=rp.device)
+        ref.index_add_(0, ridx, vals[:, None] * X64[col])
+        got = Y[:rows].double()
+        d = (got - ref)
+        return {"rows": rows, "max_rel": float(d.abs().max() / ref.abs().max()),
+                "fro_rel": float(d.norm() / ref.norm())}
 
     # CPU baseline: the oracle's restatement of the reference's CPU path
     def cpu_sample(self, max_rows):
@@ -460,8 +505,23 @@ class GatArxivTrain:
         raise NotImplementedError
 
 
+class SpmmProductsBF16(SpmmProducts):
+    """The same SpMM with BF16 features and BF16 block values."""
+    name = "spmm_products_bf16"
+    e2e_api = "att_gb300.ops.spmm (C ABI att_spmm), bf16"
+    x_kind = "bf16"
+
+
+class SpmmProductsFP8(SpmmProducts):
+    """The same SpMM with FP8 E4M3 features and per-row fp32 scales (fp16 values)."""
+    name = "spmm_products_fp8"
+    e2e_api = "att_gb300.ops.spmm (C ABI att_spmm), fp8 e4m3 + row scales"
+    x_kind = "fp8"
+
+
 WORKLOADS = {SpmmProducts.name: SpmmProducts, GatReddit.name: GatReddit,
-             GatArxivTrain.name: GatArxivTrain}
+             GatArxivTrain.name: GatArxivTrain, SpmmProductsBF16.name: SpmmProductsBF16,
+             SpmmProductsFP8.name: SpmmProductsFP8}
 DEFAULT_WORKLOAD = SpmmProducts.name
 
 
@@ -702,7 +762,8 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": wl.unit, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
                 "higher_is_better": not is_time, "scaling": "weak", "vs_baseline": None,
-                "dtype": "bf16" if "bf16" in wl.name else "f16", "data": "synthetic",
+                "dtype": "bf16" if "bf16" in wl.name else ("e4m3" if "fp8" in wl.name else "f16"),
+                "data": "synthetic",
                 "config": dict(wl.config),
                 "workload_ms_per_step": ms_per_step,
                 "roofline": roof,
@@ -717,6 +778,7 @@ def main():
                 "gflops": world * wl.flops / (ms_per_step * 1e-3) / 1e9,
                 "plain_dropin_ms_per_step": plain_ms,
                 "check_rel_err": check_err,
+                "err_vs_fp64": getattr(wl, "err_vs_fp64", None),
                 "launch_ms_p50": per_launch[len(per_launch) // 2]}
         print(json.dumps(line))
     if world > 1:

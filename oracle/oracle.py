@@ -370,3 +370,11 @@ def gat_add_layer_torch(rowptr, col, Xp, a0, a1, slope=0.2):
     p = ex / l[rows]
     out = torch.zeros(N, H, F, dtype=e.dtype).index_add(0, rows, p[:, :, None] * X3[col])
     return out.reshape(N, H * F)
+
+
+def rel_err_fro(got, ref):
+    """||got - ref||_F / ||ref||_F (Frobenius-norm relative error)."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    d = np.linalg.norm(ref)
+    return float(np.linalg.norm(got - ref) / d) if d > 0 else 0.0

@@ -121,3 +121,43 @@ def test_bad_column_sets_error_flag(cuda):
     ops.spmm(f.rowptr, col, f.val, f.window_of_part, f.atomic, X, 30, err_flag=err)
     torch.cuda.synchronize()
     assert int(err.item()) != 0
+
+
+def _quant_e4m3(X):
+    """Per-row fp32 scales and e4m3 codes (scale = max|x| / 448)."""
+    amax = X.abs().amax(1).clamp_min(1e-12)
+    scale = (amax / 448.0).float()
+    Xq = (X / scale[:, None]).to(torch.float8_e4m3fn)
+    return Xq, scale
+
+
+@pytest.mark.parametrize("W,w", [(8, 8), (16, 8), (8, 16)])
+@pytest.mark.parametrize("F", [64, 128, 256])
+def test_fp8_features_vs_fp64(cuda, W, w, F):
+    """FP8 E4M3 features with per-row fp32 scales.  The kernel: within 1e-2 of
+    the FP64 product on the dequantized features.  The format: against the
+    FP64 product on the unquantized features, Frobenius-relative error within
+    the stated FP8 tolerance 3e-2; E4M3 keeps 3 mantissa bits (rounding error
+    up to 3.1 % per element), so the max-elementwise normwise error is bounded
+    at 5e-2."""
+    from att_gb300 import graphs, ops
+    rp_t, col_t = graphs.chung_lu(3000, 12, 2.1, seed=13)
+    rowptr = graphs.pad_rows(rp_t, 8).numpy()
+    col = col_t.numpy()
+    n = 3000
+    deg = graphs.gcn_degree(torch.from_numpy(rowptr), torch.float32).numpy()
+    deg[~np.isfinite(deg)] = 0
+    deg = deg.astype(np.float16)
+    f = _format(rowptr, col, deg, W, w, 32)
+    g = torch.Generator().manual_seed(F)
+    X = torch.rand(n, F, generator=g) * 2 - 1
+    Xq, scale = _quant_e4m3(X)
+    Y = ops.spmm(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, Xq.cuda(), n, window=W,
+                 wide=w, x_scale=scale.cuda())
+    ev = oracle.gcn_values(rowptr, col, deg).astype(np.float64)
+    Xdq = (Xq.float() * scale[:, None]).double().numpy()
+    ref_q = _ref(rowptr, col, ev, Xdq, n, W)
+    assert oracle.rel_err(Y.cpu().numpy(), ref_q) <= 1e-2
+    ref = _ref(rowptr, col, ev, X.double().numpy(), n, W)
+    assert oracle.rel_err_fro(Y.cpu().numpy(), ref) <= 3e-2
+    assert oracle.rel_err(Y.cpu().numpy(), ref) <= 5e-2
