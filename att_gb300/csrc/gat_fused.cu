@@ -30,7 +30,7 @@ namespace {
 
 constexpr int kGWarps = 4;
 constexpr int kGThreads = kGWarps * 32;
-constexpr int kGStages = 4;
+constexpr int kGStages = 3;
 constexpr int kW = 8;  // window rows
 
 __device__ __forceinline__ uint32_t movmatrix_trans(uint32_t x) {

@@ -74,13 +74,13 @@ __device__ __forceinline__ int swz(int r) {
 // ---------------------------------------------------------------------------
 // 16-bit operand kernel (fp16 / bf16 values and features)
 // ---------------------------------------------------------------------------
-template <typename T, int W, int FC, int WIDE>
+template <typename T, int W, int FC, int WIDE, int S = kStages>
 struct Cfg16 {
     static constexpr int XROW = FC * 2;                 // bytes per gathered row in smem
     static constexpr int XSTAGE = 16 * XROW;            // 16 rows per k-step
     static constexpr int VSTAGE = 16 * W * 2;           // 16 cols x W rows
     static constexpr int STAGE = XSTAGE + VSTAGE;
-    static constexpr int WARP_SMEM = kStages * STAGE;
+    static constexpr int WARP_SMEM = S * STAGE;
     static constexpr int SMEM = kWarps * WARP_SMEM;
     static constexpr int CPR = FC / 8;                  // 16-byte chunks per row
     static constexpr int RPP = 32 / CPR;                // rows per warp pass
@@ -89,14 +89,14 @@ struct Cfg16 {
     static constexpr int VCH = VSTAGE / 16;             // value chunks per step
 };
 
-template <typename T, int W, int FC, int WIDE>
+template <typename T, int W, int FC, int WIDE, int S>
 __global__ void __launch_bounds__(kThreads) k_spmm16(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
     const T *__restrict__ val, const int32_t *__restrict__ win,
     const int32_t *__restrict__ atomic, int64_t n_parts, const T *__restrict__ X, int64_t n_x,
     int64_t F, int64_t ldx, float *__restrict__ Y, int64_t m_out, int64_t ldy, int n_chunks,
     int32_t *__restrict__ err) {
-    using C = Cfg16<T, W, FC, WIDE>;
+    using C = Cfg16<T, W, FC, WIDE, S>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
     p_load();
     p_fetch();
 #pragma unroll
-    for (int s = 0; s < kStages - 1; ++s) {
+    for (int s = 0; s < S - 1; ++s) {
         if (p_item < n_items) {
             issue(s);
             p_advance();
@@ -181,13 +181,13 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
 #pragma unroll
         for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
 
-    int cstage = 0, pstage = kStages - 1;
+    int cstage = 0, pstage = S - 1;
     for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
         const int64_t part = c_item / n_chunks;
         const int fc = (int)(c_item - part * n_chunks);
         const PartInfo pi = part_info<WIDE>(rowptr, part, err);
         for (int step = 0; step < pi.nsteps; ++step) {
-            cp_async_wait<kStages - 2>();
+            cp_async_wait<S - 2>();
             __syncwarp();
             const uint32_t xs = sbase + cstage * C::STAGE;
             const uint32_t vs = xs + C::XSTAGE;
@@ -222,8 +222,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
                 p_advance();
             }
             cp_async_commit();
-            cstage = cstage + 1 == kStages ? 0 : cstage + 1;
-            pstage = pstage + 1 == kStages ? 0 : pstage + 1;
+            cstage = cstage + 1 == S ? 0 : cstage + 1;
+            pstage = pstage + 1 == S ? 0 : pstage + 1;
         }
         // ---- epilogue: the W x FC tile of this part ----
         const int wrow = __ldg(win + part);
@@ -679,9 +679,9 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
 // the row's scale (done here on X, where it cannot underflow to fp16
 // subnormals as it could on the small block values) -- and runs the fp16
 // ldmatrix.trans + mma.sync path with fp32 accumulation.
-constexpr int kF8Stages = 8;
+constexpr int kF8Stages = 3;
 
-template <int W, int FC>
+template <int W, int FC, int S = kF8Stages>
 struct CfgF8 {
     static constexpr int XROW8 = FC;             // bytes per gathered e4m3 row
     static constexpr int XSTAGE = 16 * XROW8;
@@ -690,7 +690,7 @@ struct CfgF8 {
     static constexpr int STAGE = XSTAGE + VSTAGE + SSTAGE;
     static constexpr int XROW16 = FC * 2;        // dequantized fp16 tile row
     static constexpr int TILE16 = 16 * XROW16;
-    static constexpr int WARP_SMEM = kF8Stages * STAGE + TILE16;
+    static constexpr int WARP_SMEM = S * STAGE + TILE16;
     static constexpr int SMEM = kWarps * WARP_SMEM;
     static constexpr int CPR = FC / 16;          // 16-byte e4m3 chunks per row
     static constexpr int MT = FC / 16;
@@ -713,6 +713,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
     int64_t m_out, int64_t ldy, int n_chunks, int32_t *__restrict__ err) {
     using C = CfgF8<W, FC>;
     constexpr int S = kF8Stages;
+    static_assert(C::WARP_SMEM == S * C::STAGE + C::TILE16, "layout");
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
@@ -939,12 +940,12 @@ int prepare(K kernel, int smem) {
     return cuda_status(e, "cudaFuncSetAttribute");
 }
 
-template <typename T, int W, int FC, int WIDE>
+template <typename T, int W, int FC, int WIDE, int S = kStages>
 int launch16(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
              const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
              int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err, cudaStream_t st) {
-    using C = Cfg16<T, W, FC, WIDE>;
-    auto kernel = k_spmm16<T, W, FC, WIDE>;
+    using C = Cfg16<T, W, FC, WIDE, S>;
+    auto kernel = k_spmm16<T, W, FC, WIDE, S>;
     static std::once_flag once;
     static int prep = ATT_OK;
     std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
@@ -1030,6 +1031,13 @@ constexpr int kTmaStages = 5;
 // faster on the 2.45M-node graph), 1 = TMA tile::gather4.  Set through
 // att_set_option("spmm_gather", ...).
 int g_spmm_gather = 0;
+// Ring depth of the 16-bit cp.async kernel (2, 3, 4) and features per work
+// item for F > 64 (64 or 128); att_set_option("spmm_stages" / "spmm_fc").
+// Measured on the 2.45M-node graph (F = 128): throughput follows resident
+// warps per SM, not the depth of each warp's ring -- 64 features x 3 stages
+// (3.03 ms) beats 128 x 4 (4.24 ms) and 128 x 6 (5.92 ms).
+int g_spmm_stages = 3;
+int g_spmm_fc = 64;
 
 template <int W, int FC, int WIDE>
 int launch_fp8(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
@@ -1070,11 +1078,18 @@ int dispatch_fc16(const int32_t *rowptr, const int32_t *col, const void *val, co
     if (F <= 32)
         return launch16<T, W, 32, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
                                         m_out, ldy, err, st);
-    if (F <= 64)
-        return launch16<T, W, 64, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
-                                        m_out, ldy, err, st);
-    return launch16<T, W, 128, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
-                                     m_out, ldy, err, st);
+#define ATT_L16S(FCv, Sv)                                                                       \
+    return launch16<T, W, FCv, WIDE, Sv>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, \
+                                         Y, m_out, ldy, err, st)
+    if (F <= 64 || g_spmm_fc == 64) {
+        if (g_spmm_stages == 2) ATT_L16S(64, 2);
+        if (g_spmm_stages == 4) ATT_L16S(64, 4);
+        ATT_L16S(64, 3);
+    }
+    if (g_spmm_stages == 2) ATT_L16S(128, 2);
+    if (g_spmm_stages == 4) ATT_L16S(128, 4);
+    ATT_L16S(128, 3);
+#undef ATT_L16S
 }
 
 template <int W, int WIDE>
@@ -1173,14 +1188,11 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
 #define ATT_F8(Wv, FCv, WIDEv)                                                                \
     return launch_fp8<Wv, FCv, WIDEv>(rowptr, col, val, window_of_part, atomic, n_parts, X,   \
                                       x_scale, n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st)
-        if (F <= 64) {
-            if (window == 8) { if (wide == 8) ATT_F8(8, 64, 8); ATT_F8(8, 64, 16); }
-            if (wide == 8) ATT_F8(16, 64, 8);
-            ATT_F8(16, 64, 16);
-        }
-        if (window == 8) { if (wide == 8) ATT_F8(8, 128, 8); ATT_F8(8, 128, 16); }
-        if (wide == 8) ATT_F8(16, 128, 8);
-        ATT_F8(16, 128, 16);
+        // 64 features per work item: like the 16-bit kernel, throughput
+        // follows resident warps per SM
+        if (window == 8) { if (wide == 8) ATT_F8(8, 64, 8); ATT_F8(8, 64, 16); }
+        if (wide == 8) ATT_F8(16, 64, 8);
+        ATT_F8(16, 64, 16);
 #undef ATT_F8
     }
     set_error("unsupported (val_dtype=%d, x_dtype=%d) combination", val_dtype, x_dtype);
@@ -1195,6 +1207,17 @@ extern "C" int att_set_option(const char *key, int value) {
         g_spmm_gather = value;
         return ATT_OK;
     }
+    if (strcmp(key, "spmm_stages") == 0) {
+        ATT_CHECK(value == 2 || value == 3 || value == 4, ATT_ERR_INVALID,
+                  "spmm_stages must be 2, 3 or 4");
+        g_spmm_stages = value;
+        return ATT_OK;
+    }
+    if (strcmp(key, "spmm_fc") == 0) {
+        ATT_CHECK(value == 64 || value == 128, ATT_ERR_INVALID, "spmm_fc must be 64 or 128");
+        g_spmm_fc = value;
+        return ATT_OK;
+    }
     set_error("unknown option '%s'", key);
     return ATT_ERR_INVALID;
 }
@@ -1204,6 +1227,14 @@ extern "C" int att_get_option(const char *key, int *value) {
     ATT_CHECK(key != nullptr && value != nullptr, ATT_ERR_INVALID, "null argument");
     if (strcmp(key, "spmm_gather") == 0) {
         *value = g_spmm_gather;
+        return ATT_OK;
+    }
+    if (strcmp(key, "spmm_stages") == 0) {
+        *value = g_spmm_stages;
+        return ATT_OK;
+    }
+    if (strcmp(key, "spmm_fc") == 0) {
+        *value = g_spmm_fc;
         return ATT_OK;
     }
     set_error("unknown option '%s'", key);
