@@ -29,6 +29,10 @@ _SIGNATURES = {
     "att_block_plan": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int, _c_int,
                                 _c_int, _c_vp, _c_sz, ctypes.POINTER(_c_i64),
                                 ctypes.POINTER(_c_i64), _c_vp]),
+    "att_block_plan_async": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int,
+                                      _c_int, _c_int, _c_vp, _c_sz, _c_vp, _c_vp]),
+    "att_block_plan_result": (_c_int, [_c_vp, _c_i64, _c_int, ctypes.POINTER(_c_i64),
+                                       ctypes.POINTER(_c_i64)]),
     "att_block_fill": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int, _c_int,
                                 _c_int, _c_vp, _c_int, _c_vp, _c_sz, _c_vp, _c_vp, _c_vp, _c_int,
                                 _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
@@ -62,7 +66,23 @@ _SIGNATURES = {
                                   _c_vp, _c_vp, _c_int, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64, _c_vp,
                                   _c_vp, _c_vp, _c_vp, _c_vp, ctypes.c_float, _c_vp, _c_i64,
                                   _c_vp, _c_vp, _c_vp, _c_vp]),
+    "att_spmm_groups_scratch_bytes": (_c_sz, [_c_i64, _c_i64]),
+    "att_spmm_groups": (_c_int, [_c_vp, _c_i64, _c_i64, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
+                                 _c_vp, _c_sz, _c_vp]),
+    "att_spmm_batched_grid": (_c_sz, []),
+    "att_spmm_batched": (_c_int, [_c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_vp, _c_vp]),
 }
+
+
+class SpmmJob(ctypes.Structure):
+    """Mirror of att_spmm_job (include/att_gb300.h)."""
+    _fields_ = [("rowptr", _c_vp), ("col", _c_vp), ("val", _c_vp), ("window_of_part", _c_vp),
+                ("n_parts", _c_i64), ("group_part", _c_vp), ("group_slot", _c_vp),
+                ("red_first", _c_vp), ("empty_win", _c_vp), ("partial", _c_vp),
+                ("n_groups", _c_i64), ("n_red", _c_i64), ("n_slots", _c_i64), ("n_empty", _c_i64),
+                ("X", _c_vp), ("n_x", _c_i64), ("F", _c_i64), ("ldx", _c_i64), ("Y", _c_vp),
+                ("m_out", _c_i64), ("ldy", _c_i64), ("item_begin", _c_i64),
+                ("empty_begin", _c_i64), ("red_begin", _c_i64)]
 
 _lib = None
 

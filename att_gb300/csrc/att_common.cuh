@@ -50,6 +50,11 @@ inline int sm_count() {
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// In-place exclusive scan of n int64 values (convert.cu); `tmp` holds
+// scan64_tmp_bytes(n) bytes.
+size_t scan64_tmp_bytes(int64_t n);
+int scan64_exclusive(int64_t *a, int64_t n, int64_t *tmp, cudaStream_t st);
+
 // ---- device helpers -----------------------------------------------------
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {

@@ -42,6 +42,7 @@ struct Workspace {
     int64_t *part_off;   // [n_win+1]  exclusive scan of part counts
     int64_t *scan_tmp;   // [2*nblk]
     int32_t *flags;      // [4]
+    int64_t *summary;    // [3]  n_condensed, n_parts, flags (the plan's result)
     uint32_t *bitmap;    // [n_bitmap_ctas * words]
     int n_bitmap_ctas;
     int64_t words;
@@ -74,6 +75,7 @@ size_t workspace_layout(int64_t n_rows, int64_t nnz, int64_t n_cols, int window,
     size_t o_part = take((size_t)(nw + 1) * 8);
     size_t o_scan = take((size_t)(2 * nblk + 2) * 8);
     size_t o_flags = take(16);
+    size_t o_sum = take(24);
     size_t o_bitmap = take((size_t)nb * (size_t)(words > 0 ? words : 1) * 4);
     if (ws && base) {
         ws->ucols = (int32_t *)(base + o_ucols);
@@ -82,6 +84,7 @@ size_t workspace_layout(int64_t n_rows, int64_t nnz, int64_t n_cols, int window,
         ws->part_off = (int64_t *)(base + o_part);
         ws->scan_tmp = (int64_t *)(base + o_scan);
         ws->flags = (int32_t *)(base + o_flags);
+        ws->summary = (int64_t *)(base + o_sum);
         ws->bitmap = (uint32_t *)(base + o_bitmap);
         ws->n_bitmap_ctas = nb;
         ws->words = words;
@@ -449,7 +452,20 @@ __global__ void k_fill_edges(const int32_t *__restrict__ rowptr, const int32_t *
     }
 }
 
+// {n_condensed, n_parts, flags} of a finished plan, for one copy to the host
+__global__ void k_plan_summary(Workspace ws, int64_t nw) {
+    ws.summary[0] = ws.col_off[nw];
+    ws.summary[1] = ws.part_off[nw];
+    ws.summary[2] = ws.flags[0];
+}
 }  // namespace
+
+size_t scan64_tmp_bytes(int64_t n) {
+    return (size_t)((n + kScanTile - 1) / kScanTile + 1) * sizeof(int64_t);
+}
+int scan64_exclusive(int64_t *a, int64_t n, int64_t *tmp, cudaStream_t st) {
+    return exclusive_scan64(a, n, tmp, st);
+}
 }  // namespace att
 
 using namespace att;
@@ -474,20 +490,17 @@ static int check_conv_args(const int32_t *rowptr, const int32_t *col, int64_t n_
     return ATT_OK;
 }
 
-extern "C" int att_block_plan(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
-                              int64_t nnz, int64_t n_cols, int window, int wide, int part,
-                              int emit_empty, void *workspace, size_t workspace_bytes,
-                              int64_t *n_parts_out, int64_t *n_condensed_out, void *stream) {
-    clear_error();
+// Enqueue phase 1 on `st`, ending with the summary {n_condensed, n_parts,
+// flags} in ws.summary.
+static int plan_enqueue(const int32_t *rowptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                 int64_t n_cols, int window, int wide, int part, int emit_empty, void *workspace,
+                 size_t workspace_bytes, Workspace &ws, cudaStream_t st) {
     int s = check_conv_args(rowptr, col, n_rows, nnz, n_cols, window, wide, part);
     if (s != ATT_OK) return s;
-    ATT_CHECK(n_parts_out && n_condensed_out, ATT_ERR_INVALID, "null size outputs");
     size_t need = workspace_layout(n_rows, nnz, n_cols, window, nullptr, nullptr);
     ATT_CHECK(workspace != nullptr && workspace_bytes >= need, ATT_ERR_WORKSPACE,
               "workspace %zu bytes < %zu needed", workspace_bytes, need);
-    Workspace ws;
     workspace_layout(n_rows, nnz, n_cols, window, &ws, (char *)workspace);
-    cudaStream_t st = (cudaStream_t)stream;
     const int64_t nw = n_windows(n_rows, window);
     ATT_CUDA(cudaMemsetAsync(ws.flags, 0, 16, st), "memset flags");
     if (nw > 0) {
@@ -510,22 +523,63 @@ extern "C" int att_block_plan(const int32_t *rowptr, const int32_t *col, int64_t
     if (s != ATT_OK) return s;
     s = exclusive_scan64(ws.part_off, nw + 1, ws.scan_tmp, st);
     if (s != ATT_OK) return s;
-    int64_t tot[2];
-    int32_t flags[4];
-    ATT_CUDA(cudaMemcpyAsync(&tot[0], ws.col_off + nw, 8, cudaMemcpyDeviceToHost, st), "d2h");
-    ATT_CUDA(cudaMemcpyAsync(&tot[1], ws.part_off + nw, 8, cudaMemcpyDeviceToHost, st), "d2h");
-    ATT_CUDA(cudaMemcpyAsync(flags, ws.flags, 16, cudaMemcpyDeviceToHost, st), "d2h");
-    ATT_CUDA(cudaStreamSynchronize(st), "plan sync");
-    ATT_CHECK(!(flags[0] & FLAG_BAD_ROWPTR), ATT_ERR_FORMAT,
-              "rowptr is not monotone or exceeds nnz");
-    ATT_CHECK(!(flags[0] & FLAG_BAD_COL), ATT_ERR_FORMAT, "column id outside [0, %lld)",
+    k_plan_summary<<<1, 1, 0, st>>>(ws, nw);
+    return launch_status("k_plan_summary");
+}
+
+static int plan_check(const int64_t *sum, int window, int64_t n_cols, int64_t *n_parts_out,
+               int64_t *n_condensed_out) {
+    const int64_t flags = sum[2];
+    ATT_CHECK(!(flags & FLAG_BAD_ROWPTR), ATT_ERR_FORMAT, "rowptr is not monotone or exceeds nnz");
+    ATT_CHECK(!(flags & FLAG_BAD_COL), ATT_ERR_FORMAT, "column id outside [0, %lld)",
               (long long)n_cols);
-    ATT_CHECK(tot[0] * window <= INT32_MAX && 2 * tot[1] + 1 <= INT32_MAX, ATT_ERR_OVERFLOW,
+    ATT_CHECK(sum[0] * window <= INT32_MAX && 2 * sum[1] + 1 <= INT32_MAX, ATT_ERR_OVERFLOW,
               "block format would exceed int32 indexing (%lld condensed columns)",
-              (long long)tot[0]);
-    *n_condensed_out = tot[0];
-    *n_parts_out = tot[1];
+              (long long)sum[0]);
+    *n_condensed_out = sum[0];
+    *n_parts_out = sum[1];
     return ATT_OK;
+}
+
+extern "C" int att_block_plan(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
+                              int64_t nnz, int64_t n_cols, int window, int wide, int part,
+                              int emit_empty, void *workspace, size_t workspace_bytes,
+                              int64_t *n_parts_out, int64_t *n_condensed_out, void *stream) {
+    clear_error();
+    ATT_CHECK(n_parts_out && n_condensed_out, ATT_ERR_INVALID, "null size outputs");
+    cudaStream_t st = (cudaStream_t)stream;
+    Workspace ws;
+    int s = plan_enqueue(rowptr, col, n_rows, nnz, n_cols, window, wide, part, emit_empty,
+                         workspace, workspace_bytes, ws, st);
+    if (s != ATT_OK) return s;
+    int64_t sum[3];
+    ATT_CUDA(cudaMemcpyAsync(sum, ws.summary, sizeof(sum), cudaMemcpyDeviceToHost, st), "d2h");
+    ATT_CUDA(cudaStreamSynchronize(st), "plan sync");
+    return plan_check(sum, window, n_cols, n_parts_out, n_condensed_out);
+}
+
+extern "C" int att_block_plan_async(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
+                                    int64_t nnz, int64_t n_cols, int window, int wide, int part,
+                                    int emit_empty, void *workspace, size_t workspace_bytes,
+                                    int64_t *summary, void *stream) {
+    clear_error();
+    ATT_CHECK(summary != nullptr, ATT_ERR_INVALID, "null summary");
+    cudaStream_t st = (cudaStream_t)stream;
+    Workspace ws;
+    int s = plan_enqueue(rowptr, col, n_rows, nnz, n_cols, window, wide, part, emit_empty,
+                         workspace, workspace_bytes, ws, st);
+    if (s != ATT_OK) return s;
+    ATT_CUDA(cudaMemcpyAsync(summary, ws.summary, 3 * sizeof(int64_t), cudaMemcpyDefault, st),
+             "summary copy");
+    return ATT_OK;
+}
+
+extern "C" int att_block_plan_result(const int64_t *summary, int64_t n_cols, int window,
+                                     int64_t *n_parts_out, int64_t *n_condensed_out) {
+    clear_error();
+    ATT_CHECK(summary && n_parts_out && n_condensed_out && window > 0, ATT_ERR_INVALID,
+              "null argument");
+    return plan_check(summary, window, n_cols, n_parts_out, n_condensed_out);
 }
 
 extern "C" int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t n_rows,

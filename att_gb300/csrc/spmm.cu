@@ -902,6 +902,401 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
     cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// Batched SpMM over many graphs in one launch (the serving loop's kernel)
+// ---------------------------------------------------------------------------
+// The job table lives in device memory: a header {n_jobs, total items, total
+// empty windows, total multi-group windows, work counter} and, per job, the
+// block format, its groups, X and Y of one graph plus exclusive prefixes of its
+// work items (groups x feature chunks), empty windows and multi-group windows.
+// Launch parameters are only the table pointers, so one launch captured in a
+// CUDA graph can be replayed every scheduler tick after the table is
+// rewritten.  A group (<= group_parts consecutive parts of one window, chosen
+// when the groups are built) is one contiguous run of condensed columns, so it
+// streams like one long part.  Warps take work items from a queue (the
+// counter header[4]): the first item of each warp is fixed, the rest come
+// from an atomic counter, which evens out items of very different lengths
+// (one step to 16 x group_parts steps).  The per-warp cp.async pipeline runs
+// across item and job boundaries as in k_spmm16; a small per-warp ring in
+// shared memory hands the producer's item sequence to the consumer.
+
+// find the job whose [begin, next begin) range of `which` (0 items, 1 empty
+// windows, 2 multi-group windows) holds v
+__device__ __forceinline__ int64_t find_prefix(const att_spmm_job *__restrict__ jobs, int64_t n_jobs,
+                                               int64_t v, int which) {
+    int64_t lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        const int64_t b = which == 0 ? jobs[mid].item_begin
+                          : which == 1 ? jobs[mid].empty_begin : jobs[mid].red_begin;
+        if (b <= v) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Condensed-column run of parts [p0, p1) of one window.  At least one step
+// (an item whose run is empty -- only a malformed part -- streams one step
+// of zeros and stores zeros).
+template <int WIDE>
+__device__ __forceinline__ PartInfo group_info(const int32_t *__restrict__ rowptr, int64_t p0,
+                                               int64_t p1, int32_t *err) {
+    PartInfo pi;
+    pi.start = __ldg(rowptr + 2 * p0);
+    const int e = __ldg(rowptr + 2 * (p1 - 1) + 1);
+    const int pend = __ldg(rowptr + 2 * p1);
+    pi.nreal = e > pi.start ? e - pi.start : 0;
+    if ((pi.start % WIDE) != 0 || (pend % WIDE) != 0 || pend < pi.start + pi.nreal) {
+        if (err) atomicOr(err, 2);
+        pi.nreal = 0;
+    }
+    pi.nsteps = pi.nreal > 0 ? (pi.nreal + 15) >> 4 : 1;
+    return pi;
+}
+
+constexpr int kRing = 8;  // >= S + 2 items in flight per warp
+
+// 8 CTAs per SM (64 registers): like k_spmm16, throughput follows resident warps
+template <int W, int FC, int WIDE, int S>
+__global__ void __launch_bounds__(kThreads, 8) k_spmm16_batched(const att_spmm_job *__restrict__ jobs,
+                                                                int64_t *__restrict__ header,
+                                                                int32_t *__restrict__ err) {
+    static_assert(kRing >= S + 2, "item ring too small");
+    using T = __half;
+    using C = Cfg16<T, W, FC, WIDE, S>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int64_t ring[kWarps][kRing];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
+    const int64_t n_jobs = header[0];
+    const int64_t n_items = header[1];
+    unsigned long long *const counter = reinterpret_cast<unsigned long long *>(header + 4);
+    const int64_t n_fixed = (int64_t)gridDim.x * kWarps;
+    const int gid = lane >> 2, tig = lane & 3;
+    int pq = 0, cq = 0;
+
+    auto next_item = [&]() -> int64_t {
+        unsigned long long v = 0;
+        if (lane == 0) v = atomicAdd(counter, 1ull);
+        v = __shfl_sync(0xffffffffu, v, 0);
+        return n_fixed + (int64_t)v;
+    };
+
+    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    int p_step = 0, p_fc = 0, p_myc = -1;
+    PartInfo p_pi = {0, 0, 0};
+    const att_spmm_job *pj = nullptr;
+    // load item p_item (or the end marker) and hand it to the consumer
+    auto p_load = [&]() {
+        ring[warp][pq % kRing] = p_item;  // every lane writes the same value and reads its own
+        ++pq;
+        if (p_item >= n_items) return;
+        pj = jobs + find_prefix(jobs, n_jobs, p_item, 0);
+        const int64_t local = p_item - pj->item_begin;
+        const int nch = (int)((pj->F + FC - 1) / FC);
+        const int64_t g = local / nch;
+        p_fc = (int)(local - g * nch);
+        p_pi = group_info<WIDE>(pj->rowptr, __ldg(pj->group_part + g), __ldg(pj->group_part + g + 1),
+                                err);
+        p_step = 0;
+    };
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
+            p_myc = __ldg(pj->col + p_pi.start + p_step * 16 + (lane & 15));
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * C::STAGE;
+        const uint32_t vs = xs + C::XSTAGE;
+        const int c0 = p_step * 16;
+        const int myc = p_myc;
+        const T *X = (const T *)pj->X;
+        const T *val = (const T *)pj->val;
+        const int64_t fbase = (int64_t)p_fc * FC;
+#pragma unroll
+        for (int i = 0; i < 16 / C::RPP; ++i) {
+            const int r = i * C::RPP + lane / C::CPR;
+            const int ch = lane % C::CPR;
+            const int cidx = __shfl_sync(0xffffffffu, myc, r);
+            const int64_t f = fbase + ch * 8;
+            bool ok = cidx >= 0 && f < pj->F;
+            if (cidx >= pj->n_x || cidx < -1) {
+                if (err) atomicOr(err, 1);
+                ok = false;
+            }
+            const T *src = ok ? X + (int64_t)cidx * pj->ldx + f : X;
+            cp_async16(xs + r * C::XROW + ((ch ^ swz<C::XROW>(r)) << 4), src, ok ? 16 : 0);
+        }
+#pragma unroll
+        for (int q = lane; q < C::VCH; q += 32) {
+            const int e = q * 8;
+            const int blk = e / (W * WIDE);
+            const bool ok = c0 + blk * WIDE < p_pi.nreal;
+            const T *src = val + ((int64_t)(p_pi.start + c0) * W + e);
+            cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
+        }
+    };
+    auto p_advance = [&]() {
+        if (++p_step >= p_pi.nsteps) {
+            p_item = next_item();
+            p_load();
+        }
+        p_fetch();
+    };
+
+    p_load();
+    p_fetch();
+#pragma unroll
+    for (int s = 0; s < S - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+        cp_async_commit();
+    }
+
+    float acc[C::MT][C::NT][4];
+#pragma unroll
+    for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
+
+    int cstage = 0, pstage = S - 1;
+    for (;;) {
+        const int64_t c_item = ring[warp][cq % kRing];
+        ++cq;
+        if (c_item >= n_items) break;
+        const att_spmm_job *cj = jobs + find_prefix(jobs, n_jobs, c_item, 0);
+        const int64_t local = c_item - cj->item_begin;
+        const int nch = (int)((cj->F + FC - 1) / FC);
+        const int64_t g = local / nch;
+        const int fc = (int)(local - g * nch);
+        const int64_t gp0 = __ldg(cj->group_part + g);
+        const PartInfo pi = group_info<WIDE>(cj->rowptr, gp0, __ldg(cj->group_part + g + 1), nullptr);
+        for (int step = 0; step < pi.nsteps; ++step) {
+            cp_async_wait<S - 2>();
+            __syncwarp();
+            const uint32_t xs = sbase + cstage * C::STAGE;
+            const uint32_t vs = xs + C::XSTAGE;
+            uint32_t b[C::NT][2];
+            {
+                const int q = lane >> 3, rr = lane & 7;
+                if constexpr (C::NT == 2) {
+                    const int kb = q & 1, r = (q >> 1) * 8 + rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x4(vs + e * 2, b[0][0], b[0][1], b[1][0], b[1][1]);
+                } else {
+                    const int kb = q & 1, r = rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x2(vs + e * 2, b[0][0], b[0][1]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int q = lane >> 3, rr = lane & 7;
+                const int k = (q >> 1) * 8 + rr;
+                const int ch = 2 * j + (q & 1);
+                uint32_t a[4];
+                ldsm_x4_trans(xs + k * C::XROW + ((ch ^ swz<C::XROW>(k)) << 4), a[0], a[1], a[2],
+                              a[3]);
+#pragma unroll
+                for (int t = 0; t < C::NT; ++t) mma_16816<T>(acc[j][t], a, b[t][0], b[t][1]);
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                issue(pstage);
+                p_advance();
+            }
+            cp_async_commit();
+            cstage = cstage + 1 == S ? 0 : cstage + 1;
+            pstage = pstage + 1 == S ? 0 : pstage + 1;
+        }
+        const int64_t wrow = __ldg(cj->window_of_part + gp0);
+        const int slot = __ldg(cj->group_slot + g);
+        const int64_t f0 = (int64_t)fc * FC;
+        // whole window: rows of Y; else rows of partial slot `slot` ([8, F], ld F)
+        float *const base = slot < 0 ? cj->Y + wrow * W * cj->ldy : cj->partial + (int64_t)slot * W * cj->F;
+        const int64_t ld = slot < 0 ? cj->ldy : cj->F;
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) {
+            const int rl0 = t * 8 + 2 * tig;
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const int64_t fa = f0 + 16 * j + gid;
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int rl = rl0 + (h & 1);
+                    const int64_t f = fa + (h >> 1) * 8;
+                    if (rl < W && wrow * W + rl < cj->m_out && f < cj->F) base[rl * ld + f] = acc[j][t][h];
+                    acc[j][t][h] = 0.f;
+                }
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// First pass of the batched SpMM: resets the work counter and zeroes the
+// rows of windows that own no part (listed per job in empty_win; one warp per
+// window).
+template <int W>
+__global__ void k_zero_empty_batched(const att_spmm_job *__restrict__ jobs, int64_t *__restrict__ header) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) header[4] = 0;
+    const int lane = threadIdx.x & 31;
+    const int64_t n_jobs = header[0], n_e = header[2];
+    const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t ge = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ge < n_e; ge += wstride) {
+        const att_spmm_job *j = jobs + find_prefix(jobs, n_jobs, ge, 1);
+        const int64_t w = __ldg(j->empty_win + (ge - j->empty_begin));
+        const int64_t r1 = (w + 1) * W < j->m_out ? (w + 1) * W : j->m_out;
+        for (int64_t r = w * W; r < r1; ++r)
+            for (int64_t f = lane; f < j->F; f += 32) j->Y[r * j->ldy + f] = 0.f;
+    }
+}
+
+// Last pass: Y rows of a multi-group window = sum of its groups' partial slots
+// in group order.  One CTA per window; a thread per (row, 4 features).  The
+// window's slots are consecutive: [group_slot[first group], group_slot[first
+// group of the next multi-group window]) (n_slots after the last).
+template <int W>
+__global__ void __launch_bounds__(256) k_reduce_groups_batched(const att_spmm_job *__restrict__ jobs,
+                                                               const int64_t *__restrict__ header) {
+    const int64_t n_jobs = header[0], n_r = header[3];
+    for (int64_t gr = blockIdx.x; gr < n_r; gr += gridDim.x) {
+        const att_spmm_job *j = jobs + find_prefix(jobs, n_jobs, gr, 2);
+        const int64_t k = gr - j->red_begin;
+        const int g0 = __ldg(j->red_first + k);
+        const int64_t w = __ldg(j->window_of_part + __ldg(j->group_part + g0));
+        const int s0 = __ldg(j->group_slot + g0);
+        const int s1 = k + 1 < j->n_red ? __ldg(j->group_slot + __ldg(j->red_first + k + 1))
+                                        : (int)j->n_slots;
+        const int64_t F = j->F, F4 = F >> 2;
+        const float4 *part = reinterpret_cast<const float4 *>(j->partial);
+        for (int64_t u = threadIdx.x; u < W * F4; u += blockDim.x) {
+            const int64_t rl = u / F4, f4 = u - rl * F4;
+            const int64_t r = w * W + rl;
+            if (r >= j->m_out) continue;
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+            int sl = s0;
+#pragma unroll 4
+            for (; sl < s1; ++sl) {
+                const float4 v = __ldg(part + ((int64_t)sl * W + rl) * F4 + f4);
+                s.x += v.x;
+                s.y += v.y;
+                s.z += v.z;
+                s.w += v.w;
+            }
+            float *y = j->Y + r * j->ldy + f4 * 4;
+            y[0] = s.x;
+            y[1] = s.y;
+            y[2] = s.z;
+            y[3] = s.w;
+        }
+    }
+}
+
+// ---- groups of a block format -------------------------------------------------
+// Per part p of window w (parts of a window are consecutive): rank = p - first
+// part of w, np = parts of w.  p starts a group when rank % G == 0; a window
+// with np > G is multi-group: each of its groups owns a partial slot and its
+// first group opens a reduction entry.  The three flags are packed in 21-bit
+// fields of one int64 and scanned together.  Empty windows (no part) below
+// n_windows are listed by a second scan.
+constexpr int kFieldBits = 21;
+constexpr int64_t kFieldMask = (int64_t(1) << kFieldBits) - 1;
+
+__device__ __forceinline__ int64_t lower_bound_win(const int32_t *__restrict__ win, int64_t P, int64_t w) {
+    int64_t a = 0, b = P;
+    while (a < b) {
+        const int64_t m = (a + b) >> 1;
+        if (__ldg(win + m) < w) a = m + 1; else b = m;
+    }
+    return a;
+}
+
+__device__ __forceinline__ void part_rank(const int32_t *__restrict__ win, int64_t P, int64_t p,
+                                          int64_t &rank, int64_t &np) {
+    const int32_t w = __ldg(win + p);
+    int64_t a = 0, b = p;
+    while (a < b) {
+        const int64_t m = (a + b) >> 1;
+        if (__ldg(win + m) < w) a = m + 1; else b = m;
+    }
+    int64_t c = p + 1, d = P;
+    while (c < d) {
+        const int64_t m = (c + d) >> 1;
+        if (__ldg(win + m) <= w) c = m + 1; else d = m;
+    }
+    rank = p - a;
+    np = c - a;
+}
+
+__global__ void k_group_flags(const int32_t *__restrict__ win, int64_t P, int G,
+                              int64_t *__restrict__ flags) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    int64_t rank, np;
+    part_rank(win, P, p, rank, np);
+    const int64_t gs = rank % G == 0, multi = np > G;
+    flags[p] = gs | ((gs & multi) << kFieldBits) | ((int64_t)(multi && rank == 0) << (2 * kFieldBits));
+}
+
+__global__ void k_group_scatter(const int32_t *__restrict__ win, int64_t P, int G,
+                                const int64_t *__restrict__ scanned, int32_t *__restrict__ group_part,
+                                int32_t *__restrict__ group_slot, int32_t *__restrict__ red_first,
+                                int64_t *__restrict__ counts) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (P == 0) {
+        if (p == 0) {
+            group_part[0] = 0;
+            red_first[0] = 0;
+            counts[0] = counts[1] = counts[2] = 0;
+        }
+        return;
+    }
+    if (p >= P) return;
+    int64_t rank, np;
+    part_rank(win, P, p, rank, np);
+    const bool gs = rank % G == 0, multi = np > G;
+    const int64_t ex = scanned[p];
+    const int64_t gi = ex & kFieldMask, si = (ex >> kFieldBits) & kFieldMask, ri = ex >> (2 * kFieldBits);
+    if (gs) {
+        group_part[gi] = (int32_t)p;
+        group_slot[gi] = multi ? (int32_t)si : -1;
+    }
+    if (multi && rank == 0) red_first[ri] = (int32_t)gi;
+    if (p == P - 1) {
+        const int64_t ng = gi + gs, ns = si + (gs && multi), nr = ri + (multi && rank == 0);
+        group_part[ng] = (int32_t)P;
+        red_first[nr] = (int32_t)ng;
+        counts[0] = ng;
+        counts[1] = nr;
+        counts[2] = ns;
+    }
+}
+
+__global__ void k_empty_flags(const int32_t *__restrict__ win, int64_t P, int64_t n_windows,
+                              int64_t *__restrict__ flags) {
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= n_windows) return;
+    const int64_t a = lower_bound_win(win, P, w);
+    flags[w] = !(a < P && __ldg(win + a) == w);
+}
+
+__global__ void k_empty_scatter(const int32_t *__restrict__ win, int64_t P, int64_t n_windows,
+                                const int64_t *__restrict__ scanned, int32_t *__restrict__ empty_win,
+                                int64_t *__restrict__ counts) {
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_windows == 0) {
+        if (w == 0) counts[3] = 0;
+        return;
+    }
+    if (w >= n_windows) return;
+    const int64_t a = lower_bound_win(win, P, w);
+    const bool empty = !(a < P && __ldg(win + a) == w);
+    if (empty) empty_win[scanned[w]] = (int32_t)w;
+    if (w == n_windows - 1) counts[3] = scanned[w] + empty;
+}
+
 // Zero the output rows that no unsplit part writes: rows of split windows,
 // of windows without parts and rows past the last window.  One warp per window.
 __global__ void k_zero_uncovered(const int32_t *__restrict__ win, const int32_t *__restrict__ atomic,
@@ -1239,4 +1634,87 @@ extern "C" int att_get_option(const char *key, int *value) {
     }
     set_error("unknown option '%s'", key);
     return ATT_ERR_INVALID;
+}
+
+extern "C" size_t att_spmm_groups_scratch_bytes(int64_t n_parts, int64_t n_windows) {
+    if (n_parts < 0) n_parts = 0;
+    if (n_windows < 0) n_windows = 0;
+    const int64_t m = n_parts > n_windows ? n_parts : n_windows;
+    return align_up((size_t)n_parts * 8, 256) + align_up((size_t)n_windows * 8, 256) +
+           scan64_tmp_bytes(m);
+}
+
+extern "C" int att_spmm_groups(const int32_t *window_of_part, int64_t n_parts, int64_t n_windows,
+                               int group_parts, int32_t *group_part, int32_t *group_slot,
+                               int32_t *red_first, int32_t *empty_win, int64_t *counts,
+                               void *scratch, size_t scratch_bytes, void *stream) {
+    clear_error();
+    ATT_CHECK(n_parts >= 0 && n_parts < kFieldMask, ATT_ERR_UNSUPPORTED,
+              "att_spmm_groups takes fewer than %lld parts", (long long)kFieldMask);
+    ATT_CHECK(n_windows >= 0 && n_windows <= INT32_MAX, ATT_ERR_INVALID, "bad window count");
+    ATT_CHECK(group_parts >= 1 && group_parts <= 1024, ATT_ERR_INVALID,
+              "group_parts %d outside [1, 1024]", group_parts);
+    ATT_CHECK(group_part && red_first && counts, ATT_ERR_INVALID, "null output");
+    ATT_CHECK(n_parts == 0 || (window_of_part && group_slot), ATT_ERR_INVALID, "null input");
+    ATT_CHECK(n_windows == 0 || empty_win, ATT_ERR_INVALID, "null empty-window output");
+    ATT_CHECK(scratch && scratch_bytes >= att_spmm_groups_scratch_bytes(n_parts, n_windows),
+              ATT_ERR_WORKSPACE, "scratch of %zu bytes, %zu needed", scratch_bytes,
+              att_spmm_groups_scratch_bytes(n_parts, n_windows));
+    cudaStream_t st = (cudaStream_t)stream;
+    int64_t *pflags = (int64_t *)scratch;
+    int64_t *wflags = (int64_t *)((char *)scratch + align_up((size_t)n_parts * 8, 256));
+    int64_t *tmp = (int64_t *)((char *)wflags + align_up((size_t)n_windows * 8, 256));
+    const unsigned pblocks = (unsigned)((n_parts + 255) / 256);
+    const unsigned wblocks = (unsigned)((n_windows + 255) / 256);
+    int s;
+    if (n_parts > 0) {
+        k_group_flags<<<pblocks, 256, 0, st>>>(window_of_part, n_parts, group_parts, pflags);
+        if ((s = launch_status("k_group_flags")) != ATT_OK) return s;
+        if ((s = scan64_exclusive(pflags, n_parts, tmp, st)) != ATT_OK) return s;
+    }
+    k_group_scatter<<<pblocks > 0 ? pblocks : 1, 256, 0, st>>>(window_of_part, n_parts, group_parts,
+                                                               pflags, group_part, group_slot,
+                                                               red_first, counts);
+    if ((s = launch_status("k_group_scatter")) != ATT_OK) return s;
+    if (n_windows > 0) {
+        k_empty_flags<<<wblocks, 256, 0, st>>>(window_of_part, n_parts, n_windows, wflags);
+        if ((s = launch_status("k_empty_flags")) != ATT_OK) return s;
+        if ((s = scan64_exclusive(wflags, n_windows, tmp, st)) != ATT_OK) return s;
+    }
+    k_empty_scatter<<<wblocks > 0 ? wblocks : 1, 256, 0, st>>>(window_of_part, n_parts, n_windows,
+                                                               wflags, empty_win, counts);
+    return launch_status("k_empty_scatter");
+}
+
+extern "C" size_t att_spmm_batched_grid(void) {
+    using C = Cfg16<__half, 8, 64, 8, 3>;
+    auto kernel = k_spmm16_batched<8, 64, 8, 3>;
+    if (prepare(kernel, C::SMEM) != ATT_OK) return 0;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, C::SMEM);
+    return (size_t)sm_count() * (per_sm > 0 ? per_sm : 1);
+}
+
+extern "C" int att_spmm_batched(const att_spmm_job *jobs, int64_t *header, int64_t grid,
+                                int window, int wide, int32_t *err_flag, void *stream) {
+    clear_error();
+    ATT_CHECK(window == 8 && wide == 8, ATT_ERR_UNSUPPORTED,
+              "the batched SpMM takes the (8-row, 8-wide) fp16 format");
+    ATT_CHECK(jobs && header && grid > 0, ATT_ERR_INVALID, "null table or empty grid");
+    using C = Cfg16<__half, 8, 64, 8, 3>;
+    auto kernel = k_spmm16_batched<8, 64, 8, 3>;
+    static std::once_flag once;
+    static int prep = ATT_OK;
+    std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+    if (prep != ATT_OK) return prep;
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned side = (unsigned)(sm_count() * 8);
+    k_zero_empty_batched<8><<<side, 256, 0, st>>>(jobs, header);
+    int s = launch_status("k_zero_empty_batched");
+    if (s != ATT_OK) return s;
+    kernel<<<(unsigned)grid, kThreads, C::SMEM, st>>>(jobs, header, err_flag);
+    s = launch_status("k_spmm16_batched");
+    if (s != ATT_OK) return s;
+    k_reduce_groups_batched<8><<<(unsigned)(sm_count() * 4), 256, 0, st>>>(jobs, header);
+    return launch_status("k_reduce_groups_batched");
 }

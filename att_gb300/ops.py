@@ -78,16 +78,7 @@ def block_workspace_bytes(n_rows, nnz, n_cols, window):
     return int(_lib.lib().att_block_workspace_bytes(n_rows, nnz, n_cols, window))
 
 
-def block_convert(rowptr, col, deg=None, window=8, wide=8, part=32, emit_empty=False,
-                  val_dtype=None, want_val=True, want_map=False, want_trans=False,
-                  want_edge_slot=False, n_cols=None):
-    """CSR -> block format on the GPU (bit-identical to the reference CPU
-    conversion, gcn/Block_gcn/example.cpp:48-348).
-
-    ``deg``: per-node degree factor (fp16 -> fp16 values as
-    ``blockProcess_fp16_balance``; fp32 -> fp32 values as ``_tf32_balance``);
-    None for a structure/map-only format (the GAT form).
-    """
+def _conv_args(rowptr, col, deg, window, wide, part, emit_empty, val_dtype, want_val, n_cols):
     require_cuda()
     rowptr = _dev(rowptr, torch.int32)
     col = _dev(col, torch.int32)
@@ -107,33 +98,104 @@ def block_convert(rowptr, col, deg=None, window=8, wide=8, part=32, emit_empty=F
             val_dtype = deg_t.dtype
     if n_cols is None:
         n_cols = int(deg_t.shape[0]) if deg_t is not None else n_rows
-    ws_bytes = block_workspace_bytes(n_rows, nnz, n_cols, window)
-    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device="cuda")
-    n_parts = _lib.ctypes.c_int64(0)
-    n_cond = _lib.ctypes.c_int64(0)
-    st = _stream()
-    _lib.call("att_block_plan", _p(rowptr), _p(col), n_rows, nnz, n_cols, window, wide, part,
-              int(bool(emit_empty)), _p(ws), ws_bytes, _lib.ctypes.byref(n_parts),
-              _lib.ctypes.byref(n_cond), st)
-    P, NC = n_parts.value, n_cond.value
-    dev = rowptr.device
+    return dict(rowptr=rowptr, col=col, n_rows=n_rows, nnz=nnz, n_cols=n_cols, window=window,
+                wide=wide, part=part, emit_empty=int(bool(emit_empty)), deg=deg_t,
+                deg_kind=deg_kind, val_dtype=val_dtype)
+
+
+def _conv_fill(a, ws, ws_bytes, P, NC, want_map, want_trans, want_edge_slot):
+    dev = a["rowptr"].device
+    W = a["window"]
     out_rowptr = torch.empty(2 * P + 1, dtype=torch.int32, device=dev)
     out_col = torch.empty(NC, dtype=torch.int32, device=dev)
     out_win = torch.empty(P, dtype=torch.int32, device=dev)
     out_atomic = torch.empty(P, dtype=torch.int32, device=dev)
     val = None
-    if deg_t is not None:
-        val = torch.empty(NC * window, dtype=val_dtype, device=dev)
-    mp = torch.empty(NC * window, dtype=torch.int32, device=dev) if want_map else None
-    mpt = torch.empty(NC * window, dtype=torch.int32, device=dev) if want_trans else None
-    es = torch.empty(nnz, dtype=torch.int32, device=dev) if want_edge_slot else None
-    _lib.call("att_block_fill", _p(rowptr), _p(col), n_rows, nnz, n_cols, window, wide, part,
-              int(bool(emit_empty)), _p(deg_t), deg_kind, _p(ws), ws_bytes, _p(out_rowptr),
-              _p(out_col), _p(val), _DT[val_dtype] if val is not None else _lib.NONE, _p(mp),
-              _p(mpt), _p(es), _p(out_win), _p(out_atomic), st)
+    if a["deg"] is not None:
+        val = torch.empty(NC * W, dtype=a["val_dtype"], device=dev)
+    mp = torch.empty(NC * W, dtype=torch.int32, device=dev) if want_map else None
+    mpt = torch.empty(NC * W, dtype=torch.int32, device=dev) if want_trans else None
+    es = torch.empty(a["nnz"], dtype=torch.int32, device=dev) if want_edge_slot else None
+    _lib.call("att_block_fill", _p(a["rowptr"]), _p(a["col"]), a["n_rows"], a["nnz"],
+              a["n_cols"], W, a["wide"], a["part"], a["emit_empty"], _p(a["deg"]),
+              a["deg_kind"], _p(ws), ws_bytes, _p(out_rowptr), _p(out_col), _p(val),
+              _DT[a["val_dtype"]] if val is not None else _lib.NONE, _p(mp), _p(mpt), _p(es),
+              _p(out_win), _p(out_atomic), _stream())
     return BlockFormat(rowptr=out_rowptr, col=out_col, window_of_part=out_win, atomic=out_atomic,
-                       window=window, wide=wide, part=part, n_rows=n_rows, n_cols=n_cols,
-                       nnz=nnz, val=val, map=mp, map_t=mpt, edge_slot=es)
+                       window=W, wide=a["wide"], part=a["part"], n_rows=a["n_rows"],
+                       n_cols=a["n_cols"], nnz=a["nnz"], val=val, map=mp, map_t=mpt,
+                       edge_slot=es)
+
+
+def block_convert(rowptr, col, deg=None, window=8, wide=8, part=32, emit_empty=False,
+                  val_dtype=None, want_val=True, want_map=False, want_trans=False,
+                  want_edge_slot=False, n_cols=None):
+    """CSR -> block format on the GPU (bit-identical to the reference CPU
+    conversion, gcn/Block_gcn/example.cpp:48-348).
+
+    ``deg``: per-node degree factor (fp16 -> fp16 values as
+    ``blockProcess_fp16_balance``; fp32 -> fp32 values as ``_tf32_balance``);
+    None for a structure/map-only format (the GAT form).  Synchronises the
+    current stream once (the plan's sizes).
+    """
+    a = _conv_args(rowptr, col, deg, window, wide, part, emit_empty, val_dtype, want_val, n_cols)
+    ws_bytes = block_workspace_bytes(a["n_rows"], a["nnz"], a["n_cols"], window)
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device="cuda")
+    n_parts = _lib.ctypes.c_int64(0)
+    n_cond = _lib.ctypes.c_int64(0)
+    _lib.call("att_block_plan", _p(a["rowptr"]), _p(a["col"]), a["n_rows"], a["nnz"],
+              a["n_cols"], window, wide, part, a["emit_empty"], _p(ws), ws_bytes,
+              _lib.ctypes.byref(n_parts), _lib.ctypes.byref(n_cond), _stream())
+    return _conv_fill(a, ws, ws_bytes, n_parts.value, n_cond.value, want_map, want_trans,
+                      want_edge_slot)
+
+
+@dataclass
+class PendingConvert:
+    """A conversion whose plan is enqueued (block_convert_async); `event`
+    completes when the plan's summary has reached the host."""
+    args: dict
+    ws: torch.Tensor
+    ws_bytes: int
+    summary: torch.Tensor   # pinned int64 [3]
+    event: torch.cuda.Event
+    options: tuple
+
+    def ready(self):
+        return self.event.query()
+
+
+def block_convert_async(rowptr, col, deg=None, window=8, wide=8, part=32, emit_empty=False,
+                        val_dtype=None, want_val=True, want_map=False, want_trans=False,
+                        want_edge_slot=False, n_cols=None):
+    """Phase 1 of block_convert enqueued on the current stream without a
+    host synchronisation (att_block_plan_async); finish with
+    block_convert_finish once ``pending.ready()``."""
+    a = _conv_args(rowptr, col, deg, window, wide, part, emit_empty, val_dtype, want_val, n_cols)
+    ws_bytes = block_workspace_bytes(a["n_rows"], a["nnz"], a["n_cols"], window)
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device="cuda")
+    summary = torch.zeros(3, dtype=torch.int64, pin_memory=True)
+    _lib.call("att_block_plan_async", _p(a["rowptr"]), _p(a["col"]), a["n_rows"], a["nnz"],
+              a["n_cols"], window, wide, part, a["emit_empty"], _p(ws), ws_bytes, _p(summary),
+              _stream())
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream())
+    return PendingConvert(a, ws, ws_bytes, summary, ev, (want_map, want_trans, want_edge_slot))
+
+
+def block_convert_finish(pending):
+    """Phase 2: validate the plan's summary (raises AttError for a malformed
+    CSR) and enqueue the fill on the current stream (the plan's stream, or one
+    ordered after it)."""
+    if not pending.event.query():
+        raise RuntimeError("the plan has not completed: wait for pending.ready()")
+    n_parts = _lib.ctypes.c_int64(0)
+    n_cond = _lib.ctypes.c_int64(0)
+    a = pending.args
+    _lib.call("att_block_plan_result", _p(pending.summary), a["n_cols"], a["window"],
+              _lib.ctypes.byref(n_parts), _lib.ctypes.byref(n_cond))
+    return _conv_fill(a, pending.ws, pending.ws_bytes, n_parts.value, n_cond.value,
+                      *pending.options)
 
 
 def spmm(rowptr, col, val, window_of_part, atomic, X, m_out, window=8, wide=8, out=None,

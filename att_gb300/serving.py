@@ -1,0 +1,665 @@
+"""Continuous-batching GNN inference serving on one GPU.
+
+Requests are 2-layer GCN inferences, Y = A_hat relu(A_hat X W1) W2 (FP16
+features and weights, FP32 aggregation), over independent graphs.  The
+reference runs one graph per call (end2end_ori/gcn_final/eva_gcn_100.py:62-99
+loads, converts and runs each dataset in turn); this module turns that into a
+request loop:
+
+* admission -- requests are admitted in arrival order while the device-memory
+  estimate of the admitted set stays within the HBM budget and a slot is free;
+  a request larger than the whole budget, or whose graph fails validation, is
+  rejected with an error instead of blocking the queue;
+* preparation -- a worker thread per slot, each on its own CUDA stream, uploads
+  the CSR and features, converts the graph to the block format on the GPU,
+  builds its deterministic work groups (att_spmm_groups) and projects X W1;
+  the format and features then stay resident until the request completes;
+* aggregation -- every scheduler tick packs the row windows of *all* requests
+  that are ready for an aggregation (layer 1 or layer 2) into one batched SpMM
+  (att_spmm_batched), replayed from a captured CUDA graph whose kernels read a
+  device job table rewritten each tick; requests that arrive while others are
+  on the GPU join at the next tick, so their work overlaps on the device;
+* completion -- the result is copied to pinned host memory; latency is
+  arrival -> result on the host.
+
+The batched SpMM has no atomics: each request's result is bit-identical alone
+and in any mix (windows of more than four parts are summed from partial slots
+in a fixed order).  ``serve_one_by_one`` is the one-graph-per-call baseline on
+the same requests with the single-graph entry point (att_spmm).
+"""
+import ctypes
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib, graphs, ops
+from .ops import _p, _stream, require_cuda
+
+GROUP_PARTS = 4  # parts per work group of att_spmm_batched (kGroupParts in spmm.cu)
+# kernels one prepare() launches: conversion 11 (k_unique_small/large,
+# k_window_counts, two 3-kernel scans, k_fill_structure, k_fill_edges) and
+# groups 5 (k_group_flags, a 3-kernel scan, k_group_scatter); a tick launches 3
+PREPARE_LAUNCHES = 16
+TICK_LAUNCHES = 3
+ATT_ERR_FORMAT = 6
+
+
+# ---------------------------------------------------------------------------
+# requests and workload
+# ---------------------------------------------------------------------------
+@dataclass(eq=False)
+class Request:
+    rid: int
+    arrival: float                  # seconds from the start of the run
+    rowptr: torch.Tensor            # host int32 [n+1] (pinned)
+    col: torch.Tensor               # host int32 [nnz] (pinned)
+    X: torch.Tensor                 # host fp16 [n, F] (pinned)
+    n: int
+    nnz: int
+    out: Optional[torch.Tensor] = None   # host fp32 [n, F_out]
+    done_time: Optional[float] = None
+    error: Optional[str] = None
+    checksum: Optional[float] = None
+    stage: int = 0   # 0 queued, 1 preparing, 2 ready for layer 1, 3 ready for layer 2, 4 draining, 5 done
+    dev: dict = field(default_factory=dict)
+    event: Optional[torch.cuda.Event] = None
+    times: dict = field(default_factory=dict)   # host perf_counter stamps of each stage
+
+    @property
+    def latency(self):
+        return None if self.done_time is None else self.done_time - self.arrival
+
+
+def memory_estimate(n, nnz, F=128):
+    """Device bytes one request holds while admitted: the uploaded CSR, the
+    block format (a condensed column per edge at most: 4 B id + 8 fp16 values,
+    plus per-part records), group tables, features and the two layers'
+    intermediates (X W1 fp16, Y fp32, relu(Y) fp16, X2 fp16) and 1 MiB slack."""
+    csr = 4 * (n + 9) + 4 * nnz
+    fmt = 20 * nnz + 64 * (nnz // 32 + n // 8 + 8)
+    feats = n * F * (2 + 2 + 4 + 2 + 2)
+    return csr + fmt + feats + (1 << 20)
+
+
+def poisson_arrivals(rate, count, seed):
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=count))
+
+
+def graph_sizes(count, seed, n_min=1_000, n_max=500_000, deg_min=5.0, deg_max=50.0):
+    """(n, mean degree) pairs: n log-uniform in [n_min, n_max], degree uniform."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))
+        out.append((n, float(rng.uniform(deg_min, deg_max))))
+    return out
+
+
+def make_graph_pool(count, seed, F=128, gamma=2.1, device="cuda", **size_kw):
+    """Independent synthetic power-law graphs (Chung-Lu, self-loops) with
+    features uniform[-1, 1] fp16, held in pinned host memory."""
+    pool = []
+    for i, (n, deg) in enumerate(graph_sizes(count, seed, **size_kw)):
+        rp, col = graphs.chung_lu(n, deg, gamma, seed=seed * 1000 + i, device=device)
+        g = torch.Generator(device=device)
+        g.manual_seed(seed * 1000 + i)
+        X = (torch.rand(n, F, generator=g, device=device) * 2 - 1).half()
+        pool.append((rp.cpu().pin_memory(), col.cpu().pin_memory(), X.cpu().pin_memory(), n,
+                     int(col.numel())))
+    return pool
+
+
+def make_requests(pool, rate, count, seed):
+    """Poisson arrivals at `rate` per second, each on a pool graph drawn at random."""
+    arr = poisson_arrivals(rate, count, seed)
+    rng = np.random.default_rng(seed + 1)
+    reqs = []
+    for i, t in enumerate(arr):
+        rp, col, X, n, nnz = pool[int(rng.integers(0, len(pool)))]
+        reqs.append(Request(i, float(t), rp, col, X, n, nnz))
+    return reqs
+
+
+class Admission:
+    """Admits requests in arrival order while the estimated device memory of
+    the admitted set stays within ``budget`` bytes and a slot is free."""
+
+    def __init__(self, budget, max_active):
+        self.budget, self.max_active = int(budget), int(max_active)
+        self.used, self.active = 0, 0
+
+    def fits_ever(self, est):
+        return est <= self.budget
+
+    def try_admit(self, est):
+        if self.active >= self.max_active or self.used + est > self.budget:
+            return False
+        self.used += est
+        self.active += 1
+        return True
+
+    def release(self, est):
+        if est > self.used or self.active <= 0:
+            raise RuntimeError("release of %d bytes with %d admitted in %d requests"
+                               % (est, self.used, self.active))
+        self.used -= est
+        self.active -= 1
+
+
+# ---------------------------------------------------------------------------
+# groups and the batched launch
+# ---------------------------------------------------------------------------
+@dataclass
+class Groups:
+    group_part: torch.Tensor   # int32 [n_groups + 1]
+    group_slot: torch.Tensor   # int32 [n_groups]
+    red_first: torch.Tensor    # int32 [n_red + 1]
+    empty_win: torch.Tensor    # int32 [n_empty]: output windows without parts
+    n_groups: int
+    n_red: int
+    n_slots: int
+    n_empty: int
+    m_out: int                 # rows the empty-window list covers
+
+
+def _groups_enqueue(fmt, m_out, group_parts):
+    P = fmt.n_parts
+    nw = (int(m_out) + 7) // 8
+    dev = fmt.rowptr.device
+    gp = torch.empty(P + 1, dtype=torch.int32, device=dev)
+    gs = torch.empty(max(P, 1), dtype=torch.int32, device=dev)
+    rf = torch.empty(P + 1, dtype=torch.int32, device=dev)
+    ew = torch.empty(max(nw, 1), dtype=torch.int32, device=dev)
+    counts = torch.empty(4, dtype=torch.int64, device=dev)
+    nb = int(_lib.lib().att_spmm_groups_scratch_bytes(P, nw))
+    scratch = torch.empty(max(nb, 1), dtype=torch.uint8, device=dev)
+    _lib.call("att_spmm_groups", _p(fmt.window_of_part), P, nw, int(group_parts), _p(gp), _p(gs),
+              _p(rf), _p(ew), _p(counts), _p(scratch), nb, _stream())
+    return (gp, gs, rf, ew), counts
+
+
+def spmm_groups(fmt, group_parts=GROUP_PARTS, m_out=None):
+    """Work groups of a block format for the batched SpMM (att_spmm_groups)
+    writing `m_out` output rows (default: the format's rows); synchronises the
+    current stream once to read the counts."""
+    require_cuda()
+    m_out = fmt.n_rows if m_out is None else int(m_out)
+    t, counts = _groups_enqueue(fmt, m_out, group_parts)
+    ng, nr, ns, ne = (int(v) for v in counts.cpu())
+    return Groups(*t, ng, nr, ns, ne, m_out)
+
+
+@dataclass
+class PendingGroups:
+    tensors: tuple
+    counts: torch.Tensor     # pinned int64 [4]
+    event: torch.cuda.Event
+    m_out: int
+
+    def finish(self):
+        ng, nr, ns, ne = (int(v) for v in self.counts)
+        return Groups(*self.tensors, ng, nr, ns, ne, self.m_out)
+
+
+def spmm_groups_async(fmt, group_parts=GROUP_PARTS, m_out=None):
+    """spmm_groups without the synchronisation: the counts reach pinned host
+    memory when the returned ``event`` completes; then call ``finish()``."""
+    require_cuda()
+    m_out = fmt.n_rows if m_out is None else int(m_out)
+    t, counts = _groups_enqueue(fmt, m_out, group_parts)
+    host = torch.empty(4, dtype=torch.int64, pin_memory=True)
+    host.copy_(counts, non_blocking=True)
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream())
+    return PendingGroups(t, host, ev, m_out)
+
+
+@dataclass
+class Job:
+    """One graph's aggregation in a batched launch."""
+    fmt: ops.BlockFormat
+    groups: Groups
+    partial: Optional[torch.Tensor]  # fp32 with >= n_slots * 8 * F elements, or None
+    X: torch.Tensor                  # fp16 [n_x, F]
+    Y: torch.Tensor                  # fp32 [m_out, F]
+    m_out: int
+
+
+def build_job_table(jobs):
+    """Host array of att_spmm_job for `jobs` and the header (n_jobs, total
+    items, total empty windows, total multi-group windows, 0)."""
+    table = (_lib.SpmmJob * max(len(jobs), 1))()
+    items = empties = reds = 0
+    for k, jb in enumerate(jobs):
+        F = int(jb.X.shape[1])
+        if jb.X.dtype != torch.float16 or jb.X.stride(1) != 1 or jb.X.stride(0) % 8 or F % 8:
+            raise ValueError("batched SpMM features must be fp16 rows, F and stride multiples of 8")
+        if jb.Y.dtype != torch.float32 or jb.Y.stride(1) != 1 or tuple(jb.Y.shape) != (jb.m_out, F):
+            raise ValueError("batched SpMM output must be fp32 [m_out, F]")
+        if jb.fmt.window != 8 or jb.fmt.wide != 8 or jb.fmt.val is None or \
+                jb.fmt.val.dtype != torch.float16:
+            raise ValueError("batched SpMM takes the (8-row, 8-wide) fp16 block format")
+        if jb.groups.n_slots and (jb.partial is None or jb.partial.numel() < jb.groups.n_slots * 8 * F
+                                  or jb.partial.dtype != torch.float32 or jb.partial.data_ptr() % 16):
+            raise ValueError("partial buffer too small or misaligned for the job's multi-group windows")
+        if jb.groups.m_out != jb.m_out:
+            raise ValueError("groups were built for %d output rows, job has %d"
+                             % (jb.groups.m_out, jb.m_out))
+        t = table[k]
+        fmt, g = jb.fmt, jb.groups
+        t.rowptr, t.col, t.val = _p(fmt.rowptr), _p(fmt.col), _p(fmt.val)
+        t.window_of_part, t.n_parts = _p(fmt.window_of_part), fmt.n_parts
+        t.group_part, t.group_slot, t.red_first = _p(g.group_part), _p(g.group_slot), _p(g.red_first)
+        t.empty_win = _p(g.empty_win)
+        t.partial = _p(jb.partial) if jb.partial is not None else None
+        t.n_groups, t.n_red, t.n_slots, t.n_empty = g.n_groups, g.n_red, g.n_slots, g.n_empty
+        t.X, t.n_x, t.F, t.ldx = _p(jb.X), int(jb.X.shape[0]), F, int(jb.X.stride(0))
+        t.Y, t.m_out, t.ldy = _p(jb.Y), jb.m_out, int(jb.Y.stride(0))
+        t.item_begin, t.empty_begin, t.red_begin = items, empties, reds
+        items += g.n_groups * ((F + 63) // 64)
+        empties += g.n_empty
+        reds += g.n_red
+    return table, (len(jobs), items, empties, reds, 0)
+
+
+class BatchedSpmm:
+    """att_spmm_batched over a device job table.  With ``use_graph`` its three
+    kernels are captured once in a CUDA graph and replayed every call; they
+    read the job count and sizes from the device header, so one capture serves
+    every mix of jobs."""
+
+    def __init__(self, capacity, use_graph=True):
+        require_cuda()
+        self.capacity = int(capacity)
+        self.rec = ctypes.sizeof(_lib.SpmmJob)
+        self.table_d = torch.zeros(self.rec * self.capacity, dtype=torch.uint8, device="cuda")
+        self.header_d = torch.zeros(5, dtype=torch.int64, device="cuda")
+        self.err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.grid = int(_lib.lib().att_spmm_batched_grid())
+        if self.grid <= 0:
+            raise RuntimeError("att_spmm_batched_grid: no resident CTA fits: %s"
+                               % _lib.lib().att_last_error().decode())
+        self.graph = None
+        self.launches = 0
+        if use_graph:
+            self._capture()
+
+    def _launch(self):
+        _lib.call("att_spmm_batched", _p(self.table_d), _p(self.header_d), self.grid, 8, 8,
+                  _p(self.err), torch.cuda.current_stream().cuda_stream)
+
+    def _capture(self):
+        # the header is all zeros: this first launch finds no work and sets the
+        # kernel attributes outside the capture
+        self._launch()
+        torch.cuda.synchronize()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(self.graph, stream=s, capture_error_mode="thread_local"):
+                self._launch()
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+
+    def run(self, jobs):
+        """Enqueue Y_j = A_j X_j for all jobs on the current stream."""
+        if not jobs:
+            return
+        if len(jobs) > self.capacity:
+            raise ValueError("%d jobs for a table of %d" % (len(jobs), self.capacity))
+        table, header = build_job_table(jobs)
+        nb = self.rec * len(jobs)
+        # fresh pinned staging: the caching host allocator keeps a block until
+        # the copy that reads it has completed, so the next tick cannot
+        # overwrite a table still in flight
+        host = torch.empty(nb + 40, dtype=torch.uint8, pin_memory=True)
+        ctypes.memmove(host.data_ptr(), ctypes.addressof(table), nb)
+        hdr = host[nb:nb + 40].view(torch.int64)
+        hdr.copy_(torch.tensor(header, dtype=torch.int64))
+        self.table_d[:nb].copy_(host[:nb], non_blocking=True)
+        self.header_d.copy_(hdr, non_blocking=True)
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._launch()
+        self.launches += 1
+
+    def check(self):
+        """Raise if a kernel flagged a bad column id (1) or a misaligned group (2)."""
+        v = int(self.err.item())
+        if v:
+            raise _lib.AttError("att_spmm_batched", ATT_ERR_FORMAT, "device error flags 0x%x" % v)
+
+
+def spmm_batched(jobs, use_graph=False):
+    """One-shot batched SpMM over `jobs` (a list of Job) on the current stream."""
+    b = BatchedSpmm(max(len(jobs), 1), use_graph=use_graph)
+    b.run(jobs)
+    return b
+
+
+# ---------------------------------------------------------------------------
+# the model and the loop
+# ---------------------------------------------------------------------------
+class GCN2:
+    """2-layer GCN (hidden 128) with fp16 Glorot-uniform weights."""
+
+    def __init__(self, F_in=128, hidden=128, F_out=128, seed=4):
+        g = torch.Generator(device="cuda")
+        g.manual_seed(seed)
+        a1 = math.sqrt(6.0 / (F_in + hidden))
+        a2 = math.sqrt(6.0 / (hidden + F_out))
+        self.W1 = ((torch.rand(F_in, hidden, generator=g, device="cuda") * 2 - 1) * a1).half()
+        self.W2 = ((torch.rand(hidden, F_out, generator=g, device="cuda") * 2 - 1) * a2).half()
+        self.hidden, self.F_out = hidden, F_out
+
+
+def _upload_and_degree(req):
+    """Enqueue on the current stream: the request's CSR and features to the
+    device, rows padded to a multiple of 8, GCN degree factors (a node without
+    edges gets 0 instead of inf)."""
+    rp = req.rowptr.to("cuda", non_blocking=True)
+    col = req.col.to("cuda", non_blocking=True)
+    X = req.X.to("cuda", non_blocking=True)
+    rp8 = graphs.pad_rows(rp, 8)
+    deg = graphs.gcn_degree(rp8, torch.float16)
+    deg = torch.where(torch.isfinite(deg), deg, torch.zeros_like(deg))
+    return rp, col, X, rp8, deg
+
+
+def prepare(req, model, stream, with_groups=True, group_parts=GROUP_PARTS):
+    """Upload, convert, group (for the batched launch) and project one request
+    on `stream`, synchronising it twice (conversion sizes, group counts)."""
+    req.times["prep_start"] = time.perf_counter()
+    with torch.cuda.stream(stream):
+        rp, col, X, rp8, deg = _upload_and_degree(req)
+        fmt = ops.block_convert(rp8, col, deg, window=8, wide=8, part=32, n_cols=req.n)
+        groups = spmm_groups(fmt, group_parts, m_out=req.n) if with_groups else None
+        F = max(model.hidden, model.F_out)
+        partial = (torch.empty(groups.n_slots * 8 * F, dtype=torch.float32, device="cuda")
+                   if groups is not None and groups.n_slots else None)
+        X1 = torch.mm(X, model.W1)
+        Y = torch.empty(req.n, model.hidden, dtype=torch.float32, device="cuda")
+        ev = torch.cuda.Event()
+        ev.record(stream)
+    req.dev.update({"fmt": fmt, "groups": groups, "partial": partial, "X": X1, "Y": Y,
+                    "hold": [rp, col, X, rp8, deg]})
+    req.event = ev
+    req.times["prep_end"] = time.perf_counter()
+
+
+def _download(req, Y):
+    """Enqueue the copy of Y to pinned host memory, with an fp64 checksum of Y
+    computed on the device (read on the host once the copy has completed)."""
+    req.out = torch.empty(Y.shape, dtype=torch.float32, pin_memory=True)
+    req.out.copy_(Y, non_blocking=True)
+    cs = torch.empty(1, dtype=torch.float64, pin_memory=True)
+    cs.copy_(Y.sum(dtype=torch.float64).reshape(1), non_blocking=True)
+    req.dev["csum"] = cs
+
+
+def _take_checksum(req):
+    cs = req.dev.get("csum")
+    if cs is not None:
+        req.checksum = float(cs[0])
+
+
+def _job(req):
+    d = req.dev
+    return Job(d["fmt"], d["groups"], d["partial"], d["X"], d["Y"], req.n)
+
+
+class Server:
+    """The continuous-batching loop (see the module docstring), driven from
+    one host thread that never blocks on the device: every stage is enqueued
+    on a stream and advanced when its event has completed.
+
+    Request stages: plan (upload, degrees, att_block_plan_async, X W1 on a
+    preparation stream) -> fill (att_block_fill, att_spmm_groups, counts to
+    pinned memory) -> ready for layer 1 -> [tick] -> ready for layer 2 ->
+    [tick] -> download (copy stream) -> done."""
+
+    def __init__(self, model, budget=120e9, max_active=64, workers=8, use_graph=True,
+                 keep_outputs=True, max_inflight_ticks=2, group_parts=GROUP_PARTS):
+        require_cuda()
+        self.model = model
+        self.adm = Admission(budget, max_active)
+        self.workers = workers  # preparation streams (requests converting at once)
+        self.group_parts = group_parts
+        # preparation on default-priority streams; ticks and result copies on
+        # high-priority streams, so requests already on the device are not
+        # held up by new conversions
+        self.streams = [torch.cuda.Stream() for _ in range(workers)]
+        self.main = torch.cuda.Stream(priority=-1)
+        self.copy = torch.cuda.Stream(priority=-1)
+        self.batched = BatchedSpmm(max_active, use_graph=use_graph)
+        self.keep_outputs = keep_outputs
+        self.max_inflight = max_inflight_ticks
+        self.jobs_per_tick = []
+
+    def _finish(self, r, now, est):
+        r.done_time = now
+        r.times["done"] = time.perf_counter()
+        r.stage = 5
+        _take_checksum(r)
+        if not self.keep_outputs:
+            r.out = None
+        r.dev = {}
+        self.adm.release(est)
+
+    def run(self, requests, realtime=True):
+        """Serve `requests` (arrival in seconds from the call).  With
+        ``realtime=False`` every request counts as arrived at the start."""
+        with torch.cuda.stream(self.main):
+            return self._run(requests, realtime)
+
+    # -- preparation stages (on the request's stream) --------------------
+    def _start(self, r, sidx):
+        model = self.model
+        s = self.streams[sidx]
+        r.times["prep_start"] = time.perf_counter()
+        with torch.cuda.stream(s):
+            rp, col, X, rp8, deg = _upload_and_degree(r)
+            pend = ops.block_convert_async(rp8, col, deg, window=8, wide=8, part=32, n_cols=r.n)
+            X1 = torch.mm(X, model.W1)
+        r.dev.update({"sidx": sidx, "pending": pend, "X": X1, "hold": [rp, col, X, rp8, deg]})
+        r.event = pend.event
+
+    def _fill(self, r):
+        model = self.model
+        s = self.streams[r.dev["sidx"]]
+        with torch.cuda.stream(s):
+            fmt = ops.block_convert_finish(r.dev.pop("pending"))
+            pg = spmm_groups_async(fmt, self.group_parts, m_out=r.n)
+        r.dev.update({"fmt": fmt, "pgroups": pg})
+        r.event = pg.event
+
+    def _ready(self, r):
+        model = self.model
+        s = self.streams[r.dev["sidx"]]
+        g = r.dev.pop("pgroups").finish()
+        F = max(model.hidden, model.F_out)
+        with torch.cuda.stream(s):
+            partial = (torch.empty(g.n_slots * 8 * F, dtype=torch.float32, device="cuda")
+                       if g.n_slots else None)
+            Y = torch.empty(r.n, model.hidden, dtype=torch.float32, device="cuda")
+        r.dev.update({"groups": g, "partial": partial, "Y": Y, "hold": []})
+        r.times["prep_end"] = time.perf_counter()
+
+    def _run(self, requests, realtime):
+        model = self.model
+        main = self.main
+        queue = sorted(requests, key=lambda r: r.arrival)
+        qi = 0
+        planning, filling, ready1, ready2, drains, ticks = [], [], [], [], [], []
+        free_streams = list(range(self.workers))
+        ests = {}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+
+        def fail(r, e):
+            self.streams[r.dev["sidx"]].synchronize()
+            free_streams.append(r.dev["sidx"])
+            r.error = "%s: %s" % (type(e).__name__, e)
+            self._finish(r, time.perf_counter() - t0, ests.pop(r.rid))
+
+        while qi < len(queue) or planning or filling or ready1 or ready2 or drains:
+            now = time.perf_counter() - t0
+            busy = False
+            # 1. admission in arrival order, while a preparation stream is free
+            while qi < len(queue) and (not realtime or queue[qi].arrival <= now) and free_streams:
+                r = queue[qi]
+                est = memory_estimate(r.n, r.nnz, max(model.hidden, model.F_out, r.X.shape[1]))
+                if not self.adm.fits_ever(est):
+                    r.error = "needs %d bytes, over the %d-byte budget" % (est, self.adm.budget)
+                    r.stage, r.done_time = 5, now
+                    qi += 1
+                    continue
+                if not self.adm.try_admit(est):
+                    break
+                ests[r.rid] = est
+                r.stage = 1
+                r.times["admit"] = time.perf_counter()
+                sidx = free_streams.pop()
+                r.dev = {"sidx": sidx}
+                qi += 1
+                busy = True
+                try:
+                    self._start(r, sidx)
+                except Exception as e:
+                    fail(r, e)
+                    continue
+                planning.append(r)
+            # 2. plans on the host -> fill + groups
+            still = []
+            for r in planning:
+                if not r.event.query():
+                    still.append(r)
+                    continue
+                busy = True
+                try:
+                    self._fill(r)
+                except Exception as e:  # malformed CSR found by the plan
+                    fail(r, e)
+                    continue
+                filling.append(r)
+            planning = still
+            # 3. group counts on the host -> ready for layer 1
+            still = []
+            for r in filling:
+                if not r.event.query():
+                    still.append(r)
+                    continue
+                busy = True
+                self._ready(r)
+                free_streams.append(r.dev["sidx"])
+                r.stage = 2
+                ready1.append(r)
+            filling = still
+            # 4. one tick over every request ready for an aggregation
+            if ready1 or ready2:
+                if len(ticks) >= self.max_inflight:
+                    ticks.pop(0).synchronize()
+                batch1, batch2 = ready1, ready2
+                ready1, ready2 = [], []
+                t_tick = time.perf_counter()
+                for r in batch1:
+                    r.times["tick1"] = t_tick
+                for r in batch2:
+                    r.times["tick2"] = t_tick
+                self.batched.run([_job(r) for r in batch1 + batch2])
+                self.jobs_per_tick.append(len(batch1) + len(batch2))
+                agg = torch.cuda.Event()
+                agg.record(main)
+                for r in batch1:
+                    d = r.dev
+                    H = torch.relu(d["Y"]).half()
+                    d["hold"] += [d["X"], H]
+                    d["X"] = torch.mm(H, model.W2)
+                    if model.F_out != model.hidden:
+                        d["hold"].append(d["Y"])
+                        d["Y"] = torch.empty(r.n, model.F_out, dtype=torch.float32, device="cuda")
+                    r.stage = 3
+                    ready2.append(r)
+                if batch2:  # results leave on the copy stream
+                    self.copy.wait_event(agg)
+                    with torch.cuda.stream(self.copy):
+                        for r in batch2:
+                            _download(r, r.dev["Y"])
+                            ev = torch.cuda.Event()
+                            ev.record(self.copy)
+                            r.event = ev
+                            r.stage = 4
+                            drains.append(r)
+                tev = torch.cuda.Event()
+                tev.record(main)
+                ticks.append(tev)
+                busy = True
+            # 5. completions
+            still = []
+            for r in drains:
+                if r.event.query():
+                    self._finish(r, time.perf_counter() - t0, ests.pop(r.rid))
+                    busy = True
+                else:
+                    still.append(r)
+            drains = still
+            if not busy:
+                time.sleep(2e-5)
+        torch.cuda.synchronize()
+        self.batched.check()
+        return requests
+
+
+def serve(requests, model, realtime=True, **kw):
+    return Server(model, **kw).run(requests, realtime=realtime)
+
+
+def serve_one_by_one(requests, model, realtime=True, keep_outputs=True):
+    """Baseline: one graph per call.  Each request waits for the previous one;
+    upload, conversion, X W1, att_spmm, relu, X W2, att_spmm, download and a
+    synchronisation run back to back on one stream."""
+    require_cuda()
+    s = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in sorted(requests, key=lambda q: q.arrival):
+        now = time.perf_counter() - t0
+        if realtime and now < r.arrival:
+            time.sleep(r.arrival - now)
+        try:
+            prepare(r, model, s, with_groups=False)
+        except Exception as e:
+            r.error = "%s: %s" % (type(e).__name__, e)
+            r.done_time, r.stage, r.dev = time.perf_counter() - t0, 5, {}
+            continue
+        fmt = r.dev["fmt"]
+        Y = ops.spmm_format(fmt, r.dev["X"], r.n, out=r.dev["Y"])
+        H = torch.relu(Y).half()
+        X2 = torch.mm(H, model.W2)
+        Y2 = ops.spmm_format(fmt, X2, r.n)
+        _download(r, Y2)
+        s.synchronize()
+        r.done_time = time.perf_counter() - t0
+        _take_checksum(r)
+        if not keep_outputs:
+            r.out = None
+        r.dev, r.stage = {}, 5
+    return requests
+
+
+def latency_stats(requests):
+    ok = [r for r in requests if r.latency is not None and r.error is None]
+    lat = np.array([r.latency for r in ok])
+    if lat.size == 0:
+        return {"requests": 0, "rejected": len(requests)}
+    span = max(r.done_time for r in ok) - min(r.arrival for r in ok)
+    return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3), "graphs_per_s": len(lat) / max(span, 1e-9),
+            "requests": len(lat), "rejected": len(requests) - len(ok)}

@@ -101,6 +101,18 @@ ATT_API int att_block_plan(const int32_t *rowptr, const int32_t *col, int64_t n_
                    void *workspace, size_t workspace_bytes,
                    int64_t *n_parts_out, int64_t *n_condensed_out, void *stream);
 
+/* Phase 1 without the synchronisation (no counterpart in the reference):
+ * enqueues the plan and a copy of its 3-int64 summary to `summary` (pinned
+ * host memory for an asynchronous copy).  Once `stream` has passed that copy,
+ * att_block_plan_result() validates the summary (ATT_ERR_FORMAT for a bad
+ * rowptr or column, ATT_ERR_OVERFLOW) and returns the two sizes.  The
+ * workspace must stay untouched until att_block_fill has run. */
+ATT_API int att_block_plan_async(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
+                   int64_t nnz, int64_t n_cols, int window, int wide, int part, int emit_empty,
+                   void *workspace, size_t workspace_bytes, int64_t *summary, void *stream);
+ATT_API int att_block_plan_result(const int64_t *summary, int64_t n_cols, int window,
+                   int64_t *n_parts_out, int64_t *n_condensed_out);
+
 /* Phase 2: write the format.  Output sizes: rowptr 2*n_parts+1, col
  * n_condensed, val / map / map_t n_condensed*window, window_of_part and atomic
  * n_parts.  Any of val, map, map_t may be NULL to skip it.
@@ -300,6 +312,62 @@ ATT_API int att_gat_backward(const int32_t *rowptr_t, const int32_t *col_t,
                    int64_t ldd, const float *s0, const float *s1, const float *row_max,
                    const float *row_sum, const float *c, float slope, float *dXp, int64_t ldg,
                    float *ds0, float *ds1, int32_t *err_flag, void *stream);
+
+/* ======================================================================
+ * Batched SpMM over many graphs in one launch (the serving loop's kernel; no
+ * counterpart in the reference, which runs one graph per call).
+ *
+ * Work is cut into GROUPS: runs of at most group_parts consecutive parts of
+ * one window (att_spmm_groups builds them).  A window covered by one group is stored
+ * directly; a longer window's groups write partial sums to `partial` slots that
+ * a second pass adds in group order.  No atomics: Y is bit-identical whatever
+ * other jobs share the launch.
+ * ====================================================================== */
+typedef struct {
+    const int32_t *rowptr, *col;            /* block format (8-row windows, 8-wide, fp16 values) */
+    const void *val;
+    const int32_t *window_of_part;
+    int64_t n_parts;
+    const int32_t *group_part;              /* [n_groups + 1]: first part of each group, then n_parts */
+    const int32_t *group_slot;              /* [n_groups]: -1 = whole window, else partial slot */
+    const int32_t *red_first;               /* [n_red + 1]: first group of each multi-group window */
+    const int32_t *empty_win;               /* [n_empty]: output windows that own no part */
+    float *partial;                         /* [n_slots, 8, F] fp32, 16-byte aligned (null if n_slots == 0) */
+    int64_t n_groups, n_red, n_slots, n_empty;
+    const void *X;                          /* fp16 [n_x, F], F and row stride ldx multiples of 8 */
+    int64_t n_x, F, ldx;
+    float *Y;                               /* fp32 [m_out, F], row stride ldy */
+    int64_t m_out, ldy;
+    int64_t item_begin;   /* exclusive prefix of work items (n_groups * ceil(F/64)) */
+    int64_t empty_begin;  /* exclusive prefix of empty windows (n_empty) */
+    int64_t red_begin;    /* exclusive prefix of multi-group windows (n_red) */
+} att_spmm_job;
+
+/* Groups of a block format for att_spmm_batched (device arrays; stream-ordered,
+ * no host synchronisation).  Inputs: window_of_part [n_parts] (non-decreasing),
+ * n_windows = output windows (ceil(m_out / 8)), group_parts in [1, 1024].
+ * Outputs (device, caller-allocated): group_part and red_first n_parts + 1
+ * entries, group_slot max(n_parts, 1), empty_win max(n_windows, 1); `counts`
+ * (device int64[4]) receives {n_groups, n_red, n_slots, n_empty}.  `scratch`
+ * holds att_spmm_groups_scratch_bytes(n_parts, n_windows) bytes. */
+ATT_API size_t att_spmm_groups_scratch_bytes(int64_t n_parts, int64_t n_windows);
+ATT_API int att_spmm_groups(const int32_t *window_of_part, int64_t n_parts, int64_t n_windows,
+                  int group_parts, int32_t *group_part, int32_t *group_slot, int32_t *red_first,
+                  int32_t *empty_win, int64_t *counts, void *scratch, size_t scratch_bytes,
+                  void *stream);
+
+/* Grid size (persistent: SMs x resident CTAs) to launch att_spmm_batched with. */
+ATT_API size_t att_spmm_batched_grid(void);
+
+/* Y_j = A_j X_j for every job of the DEVICE table `jobs`; `header` (device,
+ * int64[5]) holds {n_jobs >= 1, total work items, total empty windows, total
+ * multi-group windows, scratch (the work-queue counter, reset by the launch)}.
+ * The launch reads the job count and sizes from device memory, so a captured
+ * CUDA graph can be replayed after the table and header are rewritten.  Every
+ * row < m_out of every Y is written.  err_flag (optional) gets bit 1 for a
+ * column id outside [0, n_x), bit 2 for a part off the 8-column grid. */
+ATT_API int att_spmm_batched(const att_spmm_job *jobs, int64_t *header, int64_t grid,
+                   int window, int wide, int32_t *err_flag, void *stream);
 
 #ifdef __cplusplus
 }

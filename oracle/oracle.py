@@ -319,8 +319,8 @@ def spmm_cpu_fp32(A, X):
 
 
 def gat_dot_layer_fp64(rowptr, col, Xp, n_out, slope=0.2):
-    """GAT layer with dot-product logits per head (BASELINE's GAT-layer
-    workload): e_ij = Xp_i . Xp_j -> LeakyReLU -> row softmax -> sum_j p_ij Xp_j.
+    """GAT layer with dot-product logits per head (the SDDMM of (XW)(XW)^T
+    masked to the edges, as in the 232,965-node GAT-layer workload): e_ij = Xp_i . Xp_j -> LeakyReLU -> row softmax -> sum_j p_ij Xp_j.
     Xp [h, M, F]."""
     e = sddmm_fp64(rowptr, col, Xp, Xp)
     e = np.where(e > 0, e, slope * e)

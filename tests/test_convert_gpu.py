@@ -113,3 +113,33 @@ def test_empty_graph(cuda):
     assert f.n_parts == 0 and f.rowptr.tolist() == [0]
     f = _gpu(rowptr, col, np.ones(16, np.float32), 8, 4, 32, True)
     assert f.n_parts == 2 and f.rowptr.tolist() == [0, 0, 0, 0, 0]
+
+
+def test_async_convert_matches_sync(cuda):
+    """block_convert_async + block_convert_finish (no host synchronisation in
+    the plan) give the same format as block_convert, bit for bit."""
+    import torch
+    from att_gb300 import graphs, ops
+    for seed, (n, L, hubs) in enumerate([(64, 8, 0), (3001, 30, 4), (20000, 12, 10)]):
+        rp, col = graphs.random_csr(n, n, L, seed, hub_rows=hubs, hub_len=min(n, 2000))
+        deg = torch.rand(n, dtype=torch.float32).half()
+        a = ops.block_convert(torch.from_numpy(rp), torch.from_numpy(col), deg, window=8, wide=8,
+                              part=32, want_map=True)
+        p = ops.block_convert_async(torch.from_numpy(rp), torch.from_numpy(col), deg, window=8,
+                                    wide=8, part=32, want_map=True)
+        p.event.synchronize()
+        b = ops.block_convert_finish(p)
+        for name in ("rowptr", "col", "window_of_part", "atomic", "val", "map"):
+            assert torch.equal(getattr(a, name), getattr(b, name)), (seed, name)
+
+
+def test_async_convert_rejects_bad_column(cuda):
+    import torch
+    from att_gb300 import ops, _lib
+    col = COL.copy()
+    col[5] = 40
+    p = ops.block_convert_async(torch.from_numpy(ROW), torch.from_numpy(col),
+                                torch.ones(32, dtype=torch.float16), window=8, wide=8, part=32)
+    p.event.synchronize()
+    with pytest.raises(_lib.AttError):
+        ops.block_convert_finish(p)
