@@ -69,6 +69,7 @@ _SIGNATURES = {
     "att_spmm_groups_scratch_bytes": (_c_sz, [_c_i64, _c_i64]),
     "att_spmm_groups": (_c_int, [_c_vp, _c_i64, _c_i64, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp,
                                  _c_vp, _c_sz, _c_vp]),
+    "att_host_device_pointer": (_c_int, [_c_vp, ctypes.POINTER(_c_vp)]),
     "att_spmm_batched_grid": (_c_sz, []),
     "att_spmm_batched": (_c_int, [_c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_vp, _c_vp]),
 }

@@ -89,29 +89,33 @@ struct Cfg16 {
     static constexpr int VCH = VSTAGE / 16;             // value chunks per step
 };
 
-template <typename T, int W, int FC, int WIDE, int S>
+// IT: index type of items and element offsets -- int32_t when every offset
+// into X, Y and the values fits (the common case: fewer instructions per
+// gathered row; the kernel is issue-bound), else int64_t.
+template <typename T, int W, int FC, int WIDE, int S, typename IT>
 __global__ void __launch_bounds__(kThreads) k_spmm16(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
     const T *__restrict__ val, const int32_t *__restrict__ win,
-    const int32_t *__restrict__ atomic, int64_t n_parts, const T *__restrict__ X, int64_t n_x,
-    int64_t F, int64_t ldx, float *__restrict__ Y, int64_t m_out, int64_t ldy, int n_chunks,
+    const int32_t *__restrict__ atomic, int64_t n_parts, const T *__restrict__ X, int64_t n_x_,
+    int64_t F_, int64_t ldx_, float *__restrict__ Y, int64_t m_out_, int64_t ldy_, int n_chunks,
     int32_t *__restrict__ err) {
     using C = Cfg16<T, W, FC, WIDE, S>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
-    const int64_t n_items = n_parts * n_chunks;
-    const int64_t stride = (int64_t)gridDim.x * kWarps;
+    const IT n_x = (IT)n_x_, F = (IT)F_, ldx = (IT)ldx_, m_out = (IT)m_out_, ldy = (IT)ldy_;
+    const IT n_items = (IT)(n_parts * n_chunks);
+    const IT stride = (IT)gridDim.x * kWarps;
     const int gid = lane >> 2, tig = lane & 3;
 
     // ---- producer cursor ----
-    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    IT p_item = (IT)blockIdx.x * kWarps + warp;
     int p_step = 0, p_myc = -1;
     PartInfo p_pi = {0, 0, 0};
     int p_fc = 0;
     auto p_load = [&]() {
         while (p_item < n_items) {
-            int64_t part = p_item / n_chunks;
+            const IT part = p_item / n_chunks;
             p_fc = (int)(p_item - part * n_chunks);
             p_pi = part_info<WIDE>(rowptr, part, err);
             p_step = 0;
@@ -124,27 +128,31 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
         const uint32_t vs = xs + C::XSTAGE;
         const int c0 = p_step * 16;
         int myc = p_myc;  // loaded one step ahead
-        const int64_t fbase = (int64_t)p_fc * FC;
+        // valid ids are -1 (padding) .. n_x - 1; an id outside is flagged and
+        // gathered as padding (zeros) -- checked once per id, not per chunk
+        if ((uint64_t)(int64_t)(myc + 1) > (uint64_t)n_x) {
+            if (err) atomicOr(err, 1);
+            myc = -1;
+        }
+        const IT fbase = (IT)p_fc * FC;
+        const bool full = fbase + FC <= F;  // the whole chunk is inside F (uniform)
 #pragma unroll
         for (int i = 0; i < 16 / C::RPP; ++i) {
             const int r = i * C::RPP + lane / C::CPR;
             const int ch = lane % C::CPR;
             const int cidx = __shfl_sync(0xffffffffu, myc, r);
-            const int64_t f = fbase + ch * 8;
-            bool ok = cidx >= 0 && f < F;
-            if (cidx >= n_x || cidx < -1) {
-                if (err) atomicOr(err, 1);
-                ok = false;
-            }
-            const T *src = ok ? X + (int64_t)cidx * ldx + f : X;
-            cp_async16(xs + r * C::XROW + ((ch ^ swz<C::XROW>(r)) << 4), src, ok ? 16 : 0);
+            const IT f = fbase + ch * 8;
+            const bool ok = cidx >= 0 && (full || f < F);
+            // padding: src-size 0 fills zeros (the source stays X's base)
+            const IT off = ok ? (IT)cidx * ldx + f : (IT)0;
+            cp_async16(xs + r * C::XROW + ((ch ^ swz<C::XROW>(r)) << 4), X + off, ok ? 16 : 0);
         }
 #pragma unroll
         for (int q = lane; q < C::VCH; q += 32) {
             const int e = q * 8;                       // element offset within the step's block run
             const int blk = e / (W * WIDE);
             const bool ok = c0 + blk * WIDE < p_pi.nreal;
-            const T *src = val + ((int64_t)(p_pi.start + c0) * W + e);
+            const T *src = val + ((IT)(p_pi.start + c0) * W + e);
             cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
         }
     };
@@ -182,8 +190,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
         for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
 
     int cstage = 0, pstage = S - 1;
-    for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
-        const int64_t part = c_item / n_chunks;
+    for (IT c_item = (IT)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const IT part = c_item / n_chunks;
         const int fc = (int)(c_item - part * n_chunks);
         const PartInfo pi = part_info<WIDE>(rowptr, part, err);
         for (int step = 0; step < pi.nsteps; ++step) {
@@ -228,19 +236,20 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
         // ---- epilogue: the W x FC tile of this part ----
         const int wrow = __ldg(win + part);
         const bool add = __ldg(atomic + part) != 0;
-        const int64_t f0 = (int64_t)fc * FC;
+        const IT f0 = (IT)fc * FC;
+        const bool full = f0 + FC <= F;
 #pragma unroll
         for (int t = 0; t < C::NT; ++t) {
-            const int64_t r0 = (int64_t)wrow * W + t * 8 + 2 * tig;
+            const IT r0 = (IT)wrow * W + t * 8 + 2 * tig;
 #pragma unroll
             for (int j = 0; j < C::MT; ++j) {
-                const int64_t fa = f0 + 16 * j + gid;
+                const IT fa = f0 + 16 * j + gid;
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    const int64_t r = r0 + (h & 1);
-                    const int64_t f = fa + (h >> 1) * 8;
-                    if (r >= 0 && r < m_out && f < F) {
-                        float *dst = Y + r * ldy + f;
+                    const IT r = r0 + (h & 1);
+                    const IT f = fa + (h >> 1) * 8;
+                    if (r < m_out && (full || f < F)) {
+                        float *dst = Y + (r * ldy + f);
                         if (add) red_add_f32(dst, acc[j][t][h]);
                         else *dst = acc[j][t][h];
                     }
@@ -1340,19 +1349,27 @@ int launch16(const int32_t *rowptr, const int32_t *col, const void *val, const i
              const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
              int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err, cudaStream_t st) {
     using C = Cfg16<T, W, FC, WIDE, S>;
-    auto kernel = k_spmm16<T, W, FC, WIDE, S>;
-    static std::once_flag once;
-    static int prep = ATT_OK;
-    std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
-    if (prep != ATT_OK) return prep;
     const int n_chunks = (int)((F + FC - 1) / FC);
     const int64_t items = n_parts * n_chunks;
     if (items == 0) return ATT_OK;
-    const int grid = occupancy_grid(kernel, C::SMEM, items);
-    kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const T *)val, win, atomic, n_parts,
-                                            (const T *)X, n_x, F, ldx, Y, m_out, ldy, n_chunks,
-                                            err);
-    return launch_status("k_spmm16");
+    // 32-bit indices when every element offset stays below 2^31: X rows
+    // (n_x * ldx), Y rows (m_out * ldy) and items (plus one grid stride of
+    // overshoot); value offsets are below 2^31 by the format's own limit
+    const int64_t lim = INT32_MAX - (1 << 22);
+    const bool small = n_x * ldx < lim && m_out * ldy < lim && items < lim;
+    auto run = [&](auto kernel) {
+        static std::once_flag once;
+        static int prep = ATT_OK;
+        std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+        if (prep != ATT_OK) return prep;
+        const int grid = occupancy_grid(kernel, C::SMEM, items);
+        kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const T *)val, win, atomic, n_parts,
+                                                (const T *)X, n_x, F, ldx, Y, m_out, ldy, n_chunks,
+                                                err);
+        return launch_status("k_spmm16");
+    };
+    if (small) return run(k_spmm16<T, W, FC, WIDE, S, int32_t>);
+    return run(k_spmm16<T, W, FC, WIDE, S, int64_t>);
 }
 
 template <int W, int FC, int WIDE>
@@ -1684,6 +1701,17 @@ extern "C" int att_spmm_groups(const int32_t *window_of_part, int64_t n_parts, i
     k_empty_scatter<<<wblocks > 0 ? wblocks : 1, 256, 0, st>>>(window_of_part, n_parts, n_windows,
                                                                wflags, empty_win, counts);
     return launch_status("k_empty_scatter");
+}
+
+extern "C" int att_host_device_pointer(const void *host, void **device) {
+    clear_error();
+    ATT_CHECK(host && device, ATT_ERR_INVALID, "null pointer");
+    cudaPointerAttributes a;
+    ATT_CUDA(cudaPointerGetAttributes(&a, host), "cudaPointerGetAttributes");
+    ATT_CHECK(a.type == cudaMemoryTypeHost && a.devicePointer != nullptr, ATT_ERR_INVALID,
+              "%p is not page-locked host memory mapped for the device", host);
+    *device = a.devicePointer;
+    return ATT_OK;
 }
 
 extern "C" size_t att_spmm_batched_grid(void) {

@@ -784,10 +784,16 @@ def run_serving(args):
         c0 = time.perf_counter()
         fn(q)
         cap[name] = len(q) / (time.perf_counter() - c0)
-    # results agree between the two paths (checksum of each output)
-    cs = np.array([r.checksum for r in reqs])
-    pcs = np.array([r.checksum for r in plain])
-    agree = float(np.max(np.abs(cs - pcs) / np.maximum(np.abs(pcs), 1.0)))
+    # results agree between the two paths: full outputs of 48 requests
+    # (untimed; the batched path is deterministic, the one-by-one path adds
+    # split windows with atomics, so they differ by fp32 rounding only)
+    vr = [serving.Request(r.rid, 0.0, r.rowptr, r.col, r.X, r.n, r.nnz) for r in reqs[:48]]
+    vp = [serving.Request(r.rid, 0.0, r.rowptr, r.col, r.X, r.n, r.nnz) for r in reqs[:48]]
+    serving.Server(model, budget=120e9, max_active=64, workers=8).run(vr, realtime=False)
+    serving.serve_one_by_one(vp, model, realtime=False)
+    agree = max(float((a.out - b.out).abs().max() / b.out.abs().max().clamp_min(1e-30))
+                for a, b in zip(vr, vp))
+    del vr, vp
     roof_raw = _batched_roofline(pool, model, max(5, min(args.steps, 20)))
     peak, peak_kind = peaks()
     achieved = roof_raw["bytes"] / (roof_raw["batched_ms"] * 1e-3) / 1e9
@@ -815,7 +821,7 @@ def run_serving(args):
                                          "mean_ms": pst["mean_ms"],
                                          "graphs_per_s": pst["graphs_per_s"]},
             "saturation_graphs_per_s": cap,
-            "checksum_max_rel_diff_vs_plain": agree,
+            "max_rel_diff_vs_plain_48_requests": agree,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                          "kernel": "att_spmm_batched over %d resident graphs (%d nodes, %d edges)"

@@ -356,6 +356,11 @@ ATT_API int att_spmm_groups(const int32_t *window_of_part, int64_t n_parts, int6
                   int32_t *empty_win, int64_t *counts, void *scratch, size_t scratch_bytes,
                   void *stream);
 
+/* Device address of page-locked (pinned) host memory, for kernels that write
+ * results straight to the host (a Y of att_spmm_batched may live there: the
+ * launch only writes Y).  ATT_ERR_INVALID if `host` is not mapped pinned memory. */
+ATT_API int att_host_device_pointer(const void *host, void **device);
+
 /* Grid size (persistent: SMs x resident CTAs) to launch att_spmm_batched with. */
 ATT_API size_t att_spmm_batched_grid(void);
 

@@ -85,7 +85,7 @@ def _fake_job(n, F, n_parts, n_groups, n_red):
     part = torch.zeros(2 * n_red * 8 * F, dtype=torch.float32) if n_red else None
     X = torch.zeros(n, F, dtype=torch.float16)
     Y = torch.zeros(n, F, dtype=torch.float32)
-    return serving.Job(fmt, g, part, X, Y, n)
+    return serving.Job(fmt, g, part, X, Y, n, y_ptr=Y.data_ptr())  # host Y: address given
 
 
 def test_job_table_prefixes():
@@ -107,6 +107,10 @@ def test_job_table_rejects_bad_jobs():
         serving.build_job_table([j])
     j = _fake_job(16, 64, 2, 2, 0)
     j.X = torch.zeros(16, 64, dtype=torch.float32)
+    with pytest.raises(ValueError):
+        serving.build_job_table([j])
+    j = _fake_job(16, 64, 2, 2, 0)
+    j.y_ptr = None  # a host Y without its device address
     with pytest.raises(ValueError):
         serving.build_job_table([j])
     j = _fake_job(16, 64, 2, 2, 0)

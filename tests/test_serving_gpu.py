@@ -231,15 +231,19 @@ def test_serving_alone_vs_mix_and_vs_one_by_one(cuda):
         srv.run([r], realtime=False)
         assert r.error is None
         alone[r.rid] = r.out.clone()
-    # in the mix: all at once, and with Poisson arrivals in real time
-    for realtime in (False, True):
+    # in the mix: all at once, with Poisson arrivals in real time, and with
+    # results copied back from device memory instead of written to the host
+    copy_srv = serving.Server(model, max_active=16, workers=4, direct_output=False, checksum=True)
+    for realtime, server in ((False, srv), (True, srv), (True, copy_srv)):
         mixed = _clone(reqs)
-        srv.run(mixed, realtime=realtime)
+        server.run(mixed, realtime=realtime)
         for r in mixed:
             assert r.error is None and r.out is not None
             ref = alone[r.rid]
             diff = (r.out - ref).abs().max().item()
             assert diff <= 1e-6 * max(ref.abs().max().item(), 1e-30), (realtime, r.rid, diff)
+            if server is copy_srv:   # device-side checksum of the copied result
+                assert abs(r.checksum - ref.double().sum().item()) <= 1e-6 * ref.abs().sum().item()
     assert max(srv.jobs_per_tick) > 1    # ticks really held several graphs
     # the one-graph-per-call path (att_spmm, split windows by atomics) agrees
     seq = serving.serve_one_by_one(_clone(reqs), model, realtime=False)
@@ -292,3 +296,20 @@ def test_serving_rejects_bad_requests_and_keeps_serving(cuda):
         if i != 2:
             assert r.error is None and r.out is not None
     assert srv.adm.used == 0 and srv.adm.active == 0
+
+
+def test_host_output_equals_device_output(cuda):
+    """A Y in pinned host memory (written over the CPU-GPU link) equals the
+    device Y bit for bit; pageable memory is refused."""
+    from att_gb300 import serving, _lib
+    d = _prepared("hubs", 1)
+    dev = _job(d)
+    serving.spmm_batched([dev]).check()
+    host = torch.full((d["n"], 128), float("nan"), pin_memory=True)
+    j = serving.Job(d["fmt"], d["groups"], d["partial"], d["X"], host, d["n"],
+                    serving.host_device_pointer(host))
+    serving.spmm_batched([j]).check()
+    torch.cuda.synchronize()
+    assert torch.equal(host, dev.Y.cpu())
+    with pytest.raises(_lib.AttError):
+        serving.host_device_pointer(torch.zeros(16))
