@@ -87,13 +87,19 @@ struct Cfg16 {
     static constexpr int MT = FC / 16;                  // m16 tiles
     static constexpr int NT = W / 8;                    // n8 tiles
     static constexpr int VCH = VSTAGE / 16;             // value chunks per step
+    // 8-row windows with <= 64 features: as many CTAs per SM as shared memory
+    // allows (228 KB per SM, 1 KB reserved per CTA; 8 for the default shape)
+    // bound the registers; other shapes keep the compiler's choice
+    static constexpr int MINB_RAW = (228 * 1024) / (SMEM + 1024);
+    static constexpr int MINB =
+        (W != 8 || FC > 64) ? 1 : (MINB_RAW < 1 ? 1 : (MINB_RAW > 8 ? 8 : MINB_RAW));
 };
 
 // IT: index type of items and element offsets -- int32_t when every offset
 // into X, Y and the values fits (the common case: fewer instructions per
 // gathered row; the kernel is issue-bound), else int64_t.
 template <typename T, int W, int FC, int WIDE, int S, typename IT>
-__global__ void __launch_bounds__(kThreads) k_spmm16(
+__global__ void __launch_bounds__(kThreads, (Cfg16<T, W, FC, WIDE, S>::MINB)) k_spmm16(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
     const T *__restrict__ val, const int32_t *__restrict__ win,
     const int32_t *__restrict__ atomic, int64_t n_parts, const T *__restrict__ X, int64_t n_x_,
@@ -136,6 +142,9 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
         }
         const IT fbase = (IT)p_fc * FC;
         const bool full = fbase + FC <= F;  // the whole chunk is inside F (uniform)
+        // CPR lanes copy one row's FC features per pass (whole 128-byte lines
+        // per instruction; spreading a row over lane pairs measured 2.4x
+        // slower on the 2.45M-node graph)
 #pragma unroll
         for (int i = 0; i < 16 / C::RPP; ++i) {
             const int r = i * C::RPP + lane / C::CPR;
@@ -261,6 +270,186 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
     cp_async_wait<0>();
 }
 
+constexpr uint32_t kMaxPolls = 1u << 24;  // bounded mbarrier waits
+
+// ---------------------------------------------------------------------------
+// 16-bit operand kernel with bulk row copies (8-row windows, 8-wide blocks,
+// 64-feature chunks)
+// ---------------------------------------------------------------------------
+// Same contraction and epilogue as k_spmm16; the producer moves each gathered
+// row's 128 bytes with one cp.async.bulk (lanes 0-15, one row each) instead of
+// eight 16-byte cp.async spread over the warp, so the issue cost per gathered
+// row drops.  Rows sit at a 144-byte pitch: the 16-byte pad keeps
+// ldmatrix.trans conflict-free without a swizzle (a bulk copy cannot swizzle)
+// and holds one 16-byte chunk of the step's value tile (chunk r = block r / 8,
+// window row r % 8), so a stage stays 16 x 144 bytes.  Each stage completes on
+// its own mbarrier (32 arrivals + the copied bytes); waits are bounded and a
+// timeout sets error bit 4.  Padding rows (column -1) and value blocks past
+// the part's real columns are zero-filled with shared stores instead of read.
+constexpr int kBulkPitch = 144;
+
+template <typename T, int S, typename IT>
+__global__ void __launch_bounds__(kThreads) k_spmm16_bulk(
+    const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+    const T *__restrict__ val, const int32_t *__restrict__ win,
+    const int32_t *__restrict__ atomic, int64_t n_parts, const T *__restrict__ X, int64_t n_x_,
+    int64_t F_, int64_t ldx_, float *__restrict__ Y, int64_t m_out_, int64_t ldy_, int n_chunks,
+    int32_t *__restrict__ err) {
+    constexpr int W = 8, WIDE = 8, FC = 64, MT = FC / 16;
+    constexpr int STAGE = 16 * kBulkPitch;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[kWarps][S];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * (S * STAGE);
+    const uint32_t bar0 = smem_u32(&bars[warp][0]);
+    const IT n_x = (IT)n_x_, F = (IT)F_, ldx = (IT)ldx_, m_out = (IT)m_out_, ldy = (IT)ldy_;
+    const IT n_items = (IT)(n_parts * n_chunks);
+    const IT stride = (IT)gridDim.x * kWarps;
+    const int gid = lane >> 2, tig = lane & 3;
+
+    if (lane == 0)
+        for (int s = 0; s < S; ++s) mbar_init(bar0 + 8 * s, 32);
+    mbar_fence_init();
+    __syncwarp();
+
+    IT p_item = (IT)blockIdx.x * kWarps + warp;
+    int p_step = 0, p_myc = -1;
+    PartInfo p_pi = {0, 0, 0};
+    int p_fc = 0;
+    auto p_load = [&]() {
+        while (p_item < n_items) {
+            const IT part = p_item / n_chunks;
+            p_fc = (int)(p_item - part * n_chunks);
+            p_pi = part_info<WIDE>(rowptr, part, err);
+            p_step = 0;
+            if (p_pi.nsteps > 0) return;
+            p_item += stride;
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * STAGE;
+        const uint32_t bar = bar0 + 8 * stage;
+        uint32_t bytes = 0;
+        if (lane < 16) {
+            const int r = lane;
+            int cidx = p_myc;  // this lane's own column id (row r of the step)
+            if ((uint64_t)(int64_t)(cidx + 1) > (uint64_t)n_x) {
+                if (err) atomicOr(err, 1);
+                cidx = -1;
+            }
+            const IT fbase = (IT)p_fc * FC;
+            const uint32_t dst = xs + r * kBulkPitch;
+            fence_proxy_async_smem();  // earlier generic reads of this stage before the async writes
+            if (cidx >= 0) {
+                const uint32_t nb = (uint32_t)(fbase + FC <= F ? FC * 2 : (F - fbase) * 2);
+                bulk_g2s(dst, X + ((IT)cidx * ldx + fbase), nb, bar);
+                bytes += nb;
+            } else {
+#pragma unroll
+                for (int q = 0; q < FC * 2 / 16; ++q)
+                    asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};\n" ::"r"(dst + 16 * q), "r"(0)
+                                 : "memory");
+            }
+            const int c0 = p_step * 16;
+            const int blk = r >> 3;  // value chunk r: block r / 8, window row r % 8
+            if (c0 + blk * WIDE < p_pi.nreal) {
+                bulk_g2s(dst + 128, val + ((IT)(p_pi.start + c0) * W + r * 8), 16, bar);
+                bytes += 16;
+            } else {
+                asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};\n" ::"r"(dst + 128), "r"(0)
+                             : "memory");
+            }
+        }
+        if (bytes)
+            mbar_arrive_expect_tx(bar, bytes);
+        else
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+    };
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
+            p_myc = __ldg(col + p_pi.start + p_step * 16 + (lane & 15));
+    };
+    auto p_advance = [&]() {
+        if (++p_step >= p_pi.nsteps) {
+            p_item += stride;
+            p_load();
+        }
+        p_fetch();
+    };
+
+    p_load();
+    p_fetch();
+#pragma unroll
+    for (int s = 0; s < S - 1; ++s)
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+
+    float acc[MT][4];
+#pragma unroll
+    for (int j = 0; j < MT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+
+    uint32_t phase = 0;  // bit s: parity of stage s's next completion
+    int cstage = 0, pstage = S - 1;
+    for (IT c_item = (IT)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const IT part = c_item / n_chunks;
+        const int fc = (int)(c_item - part * n_chunks);
+        const PartInfo pi = part_info<WIDE>(rowptr, part, nullptr);
+        for (int step = 0; step < pi.nsteps; ++step) {
+            if (!mbar_wait_bounded(bar0 + 8 * cstage, (phase >> cstage) & 1u, kMaxPolls)) {
+                if (err) atomicOr(err, 4);
+            }
+            phase ^= 1u << cstage;
+            __syncwarp();
+            const uint32_t xs = sbase + cstage * STAGE;
+            uint32_t b0, b1;
+            {
+                // B: value tile rows = window rows; matrix kb = block kb
+                const int kb = (lane >> 3) & 1, rr = lane & 7;
+                ldsm_x2(xs + (kb * 8 + rr) * kBulkPitch + 128, b0, b1);
+            }
+#pragma unroll
+            for (int j = 0; j < MT; ++j) {
+                const int q = lane >> 3, rr = lane & 7;
+                const int k = (q >> 1) * 8 + rr;
+                const int ch = 2 * j + (q & 1);
+                uint32_t a[4];
+                ldsm_x4_trans(xs + k * kBulkPitch + ch * 16, a[0], a[1], a[2], a[3]);
+                mma_16816<T>(acc[j], a, b0, b1);
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                issue(pstage);
+                p_advance();
+            }
+            cstage = cstage + 1 == S ? 0 : cstage + 1;
+            pstage = pstage + 1 == S ? 0 : pstage + 1;
+        }
+        const int wrow = __ldg(win + part);
+        const bool add = __ldg(atomic + part) != 0;
+        const IT f0 = (IT)fc * FC;
+        const bool full = f0 + FC <= F;
+        const IT r0 = (IT)wrow * W + 2 * tig;
+#pragma unroll
+        for (int j = 0; j < MT; ++j) {
+            const IT fa = f0 + 16 * j + gid;
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const IT r = r0 + (h & 1);
+                const IT f = fa + (h >> 1) * 8;
+                if (r < m_out && (full || f < F)) {
+                    float *dst = Y + (r * ldy + f);
+                    if (add) red_add_f32(dst, acc[j][h]);
+                    else *dst = acc[j][h];
+                }
+                acc[j][h] = 0.f;
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // 16-bit operand kernel fed by TMA: tile::gather4 row gathers
 // ---------------------------------------------------------------------------
@@ -278,7 +467,6 @@ __global__ void __launch_bounds__(kThreads) k_spmm16(
 // stage completes on an mbarrier carrying the byte count; every wait is
 // bounded, and a timeout raises bit 4 of err and ends the warp after draining
 // its copies in flight.
-constexpr uint32_t kMaxPolls = 1u << 24;
 constexpr int kBox = 80;            // features per TMA box
 constexpr int kPitch = kBox * 2;    // bytes per gathered row in shared memory
 constexpr int kGroup = 4 * kPitch;  // one gather4 destination (640 B, 128-aligned)
@@ -1372,6 +1560,31 @@ int launch16(const int32_t *rowptr, const int32_t *col, const void *val, const i
     return run(k_spmm16<T, W, FC, WIDE, S, int64_t>);
 }
 
+template <typename T, int S>
+int launch16_bulk(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+                  const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
+                  int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err,
+                  cudaStream_t st) {
+    constexpr int SMEM = kWarps * S * 16 * kBulkPitch;
+    const int n_chunks = (int)((F + 63) / 64);
+    const int64_t items = n_parts * n_chunks;
+    if (items == 0) return ATT_OK;
+    const int64_t lim = INT32_MAX - (1 << 22);
+    const bool small = n_x * ldx < lim && m_out * ldy < lim && items < lim;
+    auto run = [&](auto kernel) {
+        static std::once_flag once;
+        static int prep = ATT_OK;
+        std::call_once(once, [&] { prep = prepare(kernel, SMEM); });
+        if (prep != ATT_OK) return prep;
+        const int grid = occupancy_grid(kernel, SMEM, items);
+        kernel<<<grid, kThreads, SMEM, st>>>(rowptr, col, (const T *)val, win, atomic, n_parts,
+                                             (const T *)X, n_x, F, ldx, Y, m_out, ldy, n_chunks, err);
+        return launch_status("k_spmm16_bulk");
+    };
+    if (small) return run(k_spmm16_bulk<T, S, int32_t>);
+    return run(k_spmm16_bulk<T, S, int64_t>);
+}
+
 template <int W, int FC, int WIDE>
 int launch_tf32(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
                 const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
@@ -1439,8 +1652,8 @@ int launch16_tma(const int32_t *rowptr, const int32_t *col, const void *val, con
 
 constexpr int kTmaStages = 5;
 
-// Row-gather mechanism of the 16-bit kernel: 0 = cp.async (default, measured
-// faster on the 2.45M-node graph), 1 = TMA tile::gather4.  Set through
+// Row-gather mechanism of the 16-bit kernel: 0 = cp.async (default), 1 = TMA
+// tile::gather4, 2 = cp.async.bulk per row.  Set through
 // att_set_option("spmm_gather", ...).
 int g_spmm_gather = 0;
 // Ring depth of the 16-bit cp.async kernel (2, 3, 4) and features per work
@@ -1490,6 +1703,11 @@ int dispatch_fc16(const int32_t *rowptr, const int32_t *col, const void *val, co
     if (F <= 32)
         return launch16<T, W, 32, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
                                         m_out, ldy, err, st);
+    if constexpr (W == 8 && WIDE == 8) {
+        if (g_spmm_gather == 2 && (F <= 64 || g_spmm_fc == 64))
+            return launch16_bulk<T, 3>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
+                                       m_out, ldy, err, st);
+    }
 #define ATT_L16S(FCv, Sv)                                                                       \
     return launch16<T, W, FCv, WIDE, Sv>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, \
                                          Y, m_out, ldy, err, st)
@@ -1615,7 +1833,7 @@ extern "C" int att_set_option(const char *key, int value) {
     clear_error();
     ATT_CHECK(key != nullptr, ATT_ERR_INVALID, "null option name");
     if (strcmp(key, "spmm_gather") == 0) {
-        ATT_CHECK(value == 0 || value == 1, ATT_ERR_INVALID, "spmm_gather must be 0 or 1");
+        ATT_CHECK(value >= 0 && value <= 2, ATT_ERR_INVALID, "spmm_gather must be 0, 1 or 2");
         g_spmm_gather = value;
         return ATT_OK;
     }

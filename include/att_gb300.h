@@ -62,7 +62,9 @@ enum att_dtype {
 
 /* Process-wide tuning knobs (no counterpart in the reference).
  *   "spmm_gather": 0 = 16-byte cp.async row gathers (default),
- *                  1 = TMA tile::gather4 row gathers (F >= 64).
+ *                  1 = TMA tile::gather4 row gathers (F >= 64),
+ *                  2 = one cp.async.bulk per gathered row (8-row windows,
+ *                      8-wide blocks, 64-feature chunks).
  *   "spmm_stages": ring depth of the 16-bit cp.async kernel (2, 3, 4).
  *   "spmm_fc":     features per work item for F > 64 (64, the default, or 128). */
 ATT_API int att_set_option(const char *key, int value);

@@ -161,3 +161,60 @@ def test_fp8_features_vs_fp64(cuda, W, w, F):
     ref = _ref(rowptr, col, ev, X.double().numpy(), n, W)
     assert oracle.rel_err_fro(Y.cpu().numpy(), ref) <= 3e-2
     assert oracle.rel_err(Y.cpu().numpy(), ref) <= 5e-2
+
+
+@pytest.fixture
+def gather_mode():
+    """Set att_set_option("spmm_gather", mode) for a test and restore it."""
+    from att_gb300 import _lib
+    import ctypes
+    old = ctypes.c_int(0)
+    _lib.call("att_get_option", b"spmm_gather", ctypes.byref(old))
+    yield lambda m: _lib.call("att_set_option", b"spmm_gather", m)
+    _lib.call("att_set_option", b"spmm_gather", old.value)
+
+
+@pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16])
+@pytest.mark.parametrize("P", [32, 2])
+@pytest.mark.parametrize("F", [64, 72, 128, 96])
+def test_bulk_row_copies_match(cuda, gather_mode, dtype, P, F):
+    """spmm_gather = 2 (one cp.async.bulk per gathered row) gives the default
+    producer's result (same arithmetic; split windows add atomically, so
+    within fp32 rounding) and stays within 1e-2 of FP64, including partial
+    feature chunks (F = 72, 96), split windows and rows past the last window."""
+    from att_gb300 import graphs, ops
+    rowptr, col = graphs.random_csr(3003, 3003, 30, seed=P + F, hub_rows=5, hub_len=2500,
+                                    empty_frac=0.2)
+    deg = np.full(3003, 0.25, np.float16)
+    f = _format(rowptr, col, deg, 8, 8, P)
+    val = f.val if dtype == torch.float16 else f.val.to(torch.bfloat16)
+    X = torch.from_numpy(np.random.default_rng(F).uniform(-1, 1, (3003, F)).astype(np.float32))
+    X = X.to(dtype).cuda()
+    m_out = 3010
+    outs = []
+    for mode in (0, 2):
+        gather_mode(mode)
+        Y = torch.full((m_out, F), float("nan"), device="cuda")
+        ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, X, m_out, window=8, wide=8,
+                 out=Y)
+        outs.append(Y.cpu().numpy())
+    assert oracle.rel_err(outs[1], outs[0]) <= 1e-6
+    ev = oracle.gcn_values(rowptr, col, deg).astype(np.float64)
+    if dtype == torch.bfloat16:
+        ev = torch.from_numpy(ev).to(torch.bfloat16).double().numpy()
+    ref = _ref(rowptr, col, ev, X.double().cpu().numpy(), m_out, 8)
+    assert oracle.rel_err(outs[1], ref) <= 1e-2
+    assert np.all(outs[1][3000:] == 0)
+
+
+def test_bulk_row_copies_flag_bad_column(cuda, gather_mode):
+    from att_gb300 import ops
+    gather_mode(2)
+    f = _format(ROW, COL, np.ones(32, np.float16), 8, 8, 32)
+    col = f.col.clone()
+    col[3] = 1000
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    X = torch.ones(30, 64, dtype=torch.float16, device="cuda")
+    Y = ops.spmm(f.rowptr, col, f.val, f.window_of_part, f.atomic, X, 30, err_flag=err)
+    torch.cuda.synchronize()
+    assert int(err.item()) & 1 and bool(torch.isfinite(Y).all())
