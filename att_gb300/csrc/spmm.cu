@@ -901,13 +901,15 @@ __device__ __forceinline__ uint32_t e4m3x2_to_f16x2(uint16_t v) {
     return r;
 }
 
-template <int W, int FC, int WIDE>
+// IT: index type of items and element offsets (int32_t when they fit)
+template <int W, int FC, int WIDE, typename IT>
 __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
     const __half *__restrict__ val, const int32_t *__restrict__ win,
     const int32_t *__restrict__ atomic, int64_t n_parts, const uint8_t *__restrict__ X,
-    const float *__restrict__ xscale, int64_t n_x, int64_t F, int64_t ldx, float *__restrict__ Y,
-    int64_t m_out, int64_t ldy, int n_chunks, int32_t *__restrict__ err) {
+    const float *__restrict__ xscale, int64_t n_x_, int64_t F_, int64_t ldx_, float *__restrict__ Y,
+    int64_t m_out_, int64_t ldy_, int n_chunks, int32_t *__restrict__ err) {
+    const IT n_x = (IT)n_x_, F = (IT)F_, ldx = (IT)ldx_, m_out = (IT)m_out_, ldy = (IT)ldy_;
     using C = CfgF8<W, FC>;
     constexpr int S = kF8Stages;
     static_assert(C::WARP_SMEM == S * C::STAGE + C::TILE16, "layout");
@@ -916,16 +918,16 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
     const unsigned char *sgen = smem + warp * C::WARP_SMEM;
     const uint32_t tile = sbase + S * C::STAGE;
-    const int64_t n_items = n_parts * n_chunks;
-    const int64_t stride = (int64_t)gridDim.x * kWarps;
+    const IT n_items = (IT)(n_parts * n_chunks);
+    const IT stride = (IT)gridDim.x * kWarps;
     const int gid = lane >> 2, tig = lane & 3;
 
-    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    IT p_item = (IT)blockIdx.x * kWarps + warp;
     int p_step = 0, p_fc = 0, p_myc = -1;
     PartInfo p_pi = {0, 0, 0};
     auto p_load = [&]() {
         while (p_item < n_items) {
-            int64_t part = p_item / n_chunks;
+            const IT part = p_item / n_chunks;
             p_fc = (int)(p_item - part * n_chunks);
             p_pi = part_info<WIDE>(rowptr, part, err);
             p_step = 0;
@@ -939,26 +941,28 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
         const uint32_t ss = vs + C::VSTAGE;
         const int c0 = p_step * 16;
         int myc = p_myc;  // loaded one step ahead
-        if (myc >= n_x || myc < -1) {
+        if ((uint64_t)(int64_t)(myc + 1) > (uint64_t)n_x) {  // valid: -1 .. n_x - 1
             if (err) atomicOr(err, 1);
             myc = -1;
         }
-        const int64_t fbase = (int64_t)p_fc * FC;
+        const IT fbase = (IT)p_fc * FC;
+        const bool full = fbase + FC <= F;
 #pragma unroll
         for (int i = 0; i < 16 * C::CPR / 32; ++i) {
             const int idx = i * 32 + lane;
             const int r = idx / C::CPR, ch = idx % C::CPR;
             const int cidx = __shfl_sync(0xffffffffu, myc, r);
-            const int64_t f = fbase + ch * 16;
-            const bool ok = cidx >= 0 && f < F;
-            cp_async16(xs + r * C::XROW8 + ch * 16, ok ? X + (int64_t)cidx * ldx + f : X, ok ? 16 : 0);
+            const IT f = fbase + ch * 16;
+            const bool ok = cidx >= 0 && (full || f < F);
+            const IT off = ok ? (IT)cidx * ldx + f : (IT)0;
+            cp_async16(xs + r * C::XROW8 + ch * 16, X + off, ok ? 16 : 0);
         }
 #pragma unroll
         for (int q = lane; q < C::VCH; q += 32) {
             const int e = q * 8;
             const int blk = e / (W * WIDE);
             const bool ok = c0 + blk * WIDE < p_pi.nreal;
-            const __half *src = val + ((int64_t)(p_pi.start + c0) * W + e);
+            const __half *src = val + ((IT)(p_pi.start + c0) * W + e);
             cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
         }
         if (lane < 16) {
@@ -1000,8 +1004,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
         for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
 
     int cstage = 0, pstage = S - 1;
-    for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
-        const int64_t part = c_item / n_chunks;
+    for (IT c_item = (IT)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const IT part = c_item / n_chunks;
         const int fc = (int)(c_item - part * n_chunks);
         const PartInfo pi = part_info<WIDE>(rowptr, part, nullptr);
         for (int step = 0; step < pi.nsteps; ++step) {
@@ -1075,19 +1079,20 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
         }
         const int wrow = __ldg(win + part);
         const bool add = __ldg(atomic + part) != 0;
-        const int64_t f0 = (int64_t)fc * FC;
+        const IT f0 = (IT)fc * FC;
+        const bool full = f0 + FC <= F;
 #pragma unroll
         for (int t = 0; t < C::NT; ++t) {
-            const int64_t r0 = (int64_t)wrow * W + t * 8 + 2 * tig;
+            const IT r0 = (IT)wrow * W + t * 8 + 2 * tig;
 #pragma unroll
             for (int j = 0; j < C::MT; ++j) {
-                const int64_t fa = f0 + 16 * j + gid;
+                const IT fa = f0 + 16 * j + gid;
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
-                    const int64_t r = r0 + (h & 1);
-                    const int64_t f = fa + (h >> 1) * 8;
-                    if (r >= 0 && r < m_out && f < F) {
-                        float *dst = Y + r * ldy + f;
+                    const IT r = r0 + (h & 1);
+                    const IT f = fa + (h >> 1) * 8;
+                    if (r < m_out && (full || f < F)) {
+                        float *dst = Y + (r * ldy + f);
                         if (add) red_add_f32(dst, acc[j][t][h]);
                         else *dst = acc[j][t][h];
                     }
@@ -1152,6 +1157,15 @@ __device__ __forceinline__ PartInfo group_info(const int32_t *__restrict__ rowpt
 
 constexpr int kRing = 8;  // >= S + 2 items in flight per warp
 
+// A job's element offsets (X rows, Y rows, partial slots) fit in 31 bits:
+// the batched kernel computes them in 32-bit arithmetic and skips (error bit
+// 8) a job that does not fit instead of addressing it.
+__device__ __forceinline__ bool job_small(const att_spmm_job *j) {
+    const int64_t lim = (int64_t)INT32_MAX - 4096;
+    return j->n_x * j->ldx < lim && j->m_out * j->ldy < lim && j->n_slots * 8 * j->F < lim &&
+           j->F < lim && j->ldx < lim && j->ldy < lim;
+}
+
 // 8 CTAs per SM (64 registers): like k_spmm16, throughput follows resident warps
 template <int W, int FC, int WIDE, int S>
 __global__ void __launch_bounds__(kThreads, 8) k_spmm16_batched(const att_spmm_job *__restrict__ jobs,
@@ -1161,75 +1175,93 @@ __global__ void __launch_bounds__(kThreads, 8) k_spmm16_batched(const att_spmm_j
     using T = __half;
     using C = Cfg16<T, W, FC, WIDE, S>;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int64_t ring[kWarps][kRing];
+    __shared__ int ring[kWarps][kRing];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
     const int64_t n_jobs = header[0];
-    const int64_t n_items = header[1];
-    unsigned long long *const counter = reinterpret_cast<unsigned long long *>(header + 4);
-    const int64_t n_fixed = (int64_t)gridDim.x * kWarps;
+    const int n_fixed = (int)gridDim.x * kWarps;
+    if (header[1] > (int64_t)INT32_MAX - n_fixed - 1) {  // items must be 32-bit
+        if (err && threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, 8);
+        return;
+    }
+    const int n_items = (int)header[1];
+    unsigned int *const counter = reinterpret_cast<unsigned int *>(header + 4);
     const int gid = lane >> 2, tig = lane & 3;
     int pq = 0, cq = 0;
 
-    auto next_item = [&]() -> int64_t {
-        unsigned long long v = 0;
-        if (lane == 0) v = atomicAdd(counter, 1ull);
+    auto next_item = [&]() -> int {
+        unsigned int v = 0;
+        if (lane == 0) v = atomicAdd(counter, 1u);
         v = __shfl_sync(0xffffffffu, v, 0);
-        return n_fixed + (int64_t)v;
+        return n_fixed + (int)v;
     };
 
-    int64_t p_item = (int64_t)blockIdx.x * kWarps + warp;
+    // producer cursor and the fields of its job it uses every step
+    int p_item = (int)blockIdx.x * kWarps + warp;
     int p_step = 0, p_fc = 0, p_myc = -1;
     PartInfo p_pi = {0, 0, 0};
-    const att_spmm_job *pj = nullptr;
+    const T *p_X = nullptr, *p_val = nullptr;  // p_val: the group's first value
+    const int32_t *p_col = nullptr;             // the group's first column id
+    int p_ldx = 0, p_nx = 0, p_F = 0;
     // load item p_item (or the end marker) and hand it to the consumer
     auto p_load = [&]() {
         ring[warp][pq % kRing] = p_item;  // every lane writes the same value and reads its own
         ++pq;
         if (p_item >= n_items) return;
-        pj = jobs + find_prefix(jobs, n_jobs, p_item, 0);
-        const int64_t local = p_item - pj->item_begin;
-        const int nch = (int)((pj->F + FC - 1) / FC);
-        const int64_t g = local / nch;
-        p_fc = (int)(local - g * nch);
+        const att_spmm_job *pj = jobs + find_prefix(jobs, n_jobs, p_item, 0);
+        const int local = (int)(p_item - pj->item_begin);
+        p_F = (int)pj->F;
+        const int nch = (p_F + FC - 1) / FC;
+        const int g = local / nch;
+        p_fc = local - g * nch;
+        p_X = (const T *)pj->X;
+        p_ldx = (int)pj->ldx;
+        p_nx = (int)pj->n_x;
         p_pi = group_info<WIDE>(pj->rowptr, __ldg(pj->group_part + g), __ldg(pj->group_part + g + 1),
                                 err);
+        p_val = (const T *)pj->val + p_pi.start * W;
+        p_col = pj->col + p_pi.start;
+        if (!job_small(pj)) {  // not addressed: one zero step, no store
+            if (err) atomicOr(err, 8);
+            p_pi.nreal = 0;
+            p_pi.nsteps = 1;
+        }
         p_step = 0;
     };
     auto p_fetch = [&]() {
         p_myc = -1;
         if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
-            p_myc = __ldg(pj->col + p_pi.start + p_step * 16 + (lane & 15));
+            p_myc = __ldg(p_col + p_step * 16 + (lane & 15));
     };
     auto issue = [&](int stage) {
         const uint32_t xs = sbase + stage * C::STAGE;
         const uint32_t vs = xs + C::XSTAGE;
         const int c0 = p_step * 16;
-        const int myc = p_myc;
-        const T *X = (const T *)pj->X;
-        const T *val = (const T *)pj->val;
-        const int64_t fbase = (int64_t)p_fc * FC;
+        int myc = p_myc;
+        // valid ids are -1 (padding) .. n_x - 1: checked once per id
+        if ((unsigned)(myc + 1) > (unsigned)p_nx) {
+            if (err) atomicOr(err, 1);
+            myc = -1;
+        }
+        const int fbase = p_fc * FC;
+        const bool full = fbase + FC <= p_F;
 #pragma unroll
         for (int i = 0; i < 16 / C::RPP; ++i) {
             const int r = i * C::RPP + lane / C::CPR;
             const int ch = lane % C::CPR;
             const int cidx = __shfl_sync(0xffffffffu, myc, r);
-            const int64_t f = fbase + ch * 8;
-            bool ok = cidx >= 0 && f < pj->F;
-            if (cidx >= pj->n_x || cidx < -1) {
-                if (err) atomicOr(err, 1);
-                ok = false;
-            }
-            const T *src = ok ? X + (int64_t)cidx * pj->ldx + f : X;
-            cp_async16(xs + r * C::XROW + ((ch ^ swz<C::XROW>(r)) << 4), src, ok ? 16 : 0);
+            const int f = fbase + ch * 8;
+            const bool ok = cidx >= 0 && (full || f < p_F);
+            const int off = ok ? cidx * p_ldx + f : 0;
+            cp_async16(xs + r * C::XROW + ((ch ^ swz<C::XROW>(r)) << 4), p_X + off, ok ? 16 : 0);
         }
 #pragma unroll
         for (int q = lane; q < C::VCH; q += 32) {
             const int e = q * 8;
             const int blk = e / (W * WIDE);
             const bool ok = c0 + blk * WIDE < p_pi.nreal;
-            const T *src = val + ((int64_t)(p_pi.start + c0) * W + e);
-            cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
+            const T *src = p_val + (c0 * W + e);
+            cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)p_val, ok ? 16 : 0);
         }
     };
     auto p_advance = [&]() {
@@ -1259,16 +1291,19 @@ __global__ void __launch_bounds__(kThreads, 8) k_spmm16_batched(const att_spmm_j
 
     int cstage = 0, pstage = S - 1;
     for (;;) {
-        const int64_t c_item = ring[warp][cq % kRing];
+        const int c_item = ring[warp][cq % kRing];
         ++cq;
         if (c_item >= n_items) break;
         const att_spmm_job *cj = jobs + find_prefix(jobs, n_jobs, c_item, 0);
-        const int64_t local = c_item - cj->item_begin;
-        const int nch = (int)((cj->F + FC - 1) / FC);
-        const int64_t g = local / nch;
-        const int fc = (int)(local - g * nch);
-        const int64_t gp0 = __ldg(cj->group_part + g);
-        const PartInfo pi = group_info<WIDE>(cj->rowptr, gp0, __ldg(cj->group_part + g + 1), nullptr);
+        const int local = (int)(c_item - cj->item_begin);
+        const int F = (int)cj->F;
+        const int nch = (F + FC - 1) / FC;
+        const int g = local / nch;
+        const int fc = local - g * nch;
+        const int gp0 = __ldg(cj->group_part + g);
+        PartInfo pi = group_info<WIDE>(cj->rowptr, gp0, __ldg(cj->group_part + g + 1), nullptr);
+        const bool small = job_small(cj);
+        if (!small) pi.nsteps = 1;  // the producer streamed one zero step
         for (int step = 0; step < pi.nsteps; ++step) {
             cp_async_wait<S - 2>();
             __syncwarp();
@@ -1307,23 +1342,26 @@ __global__ void __launch_bounds__(kThreads, 8) k_spmm16_batched(const att_spmm_j
             cstage = cstage + 1 == S ? 0 : cstage + 1;
             pstage = pstage + 1 == S ? 0 : pstage + 1;
         }
-        const int64_t wrow = __ldg(cj->window_of_part + gp0);
+        const int wrow = __ldg(cj->window_of_part + gp0);
         const int slot = __ldg(cj->group_slot + g);
-        const int64_t f0 = (int64_t)fc * FC;
+        const int f0 = fc * FC;
+        const bool full = f0 + FC <= F;
+        const int m_out = (int)cj->m_out;
         // whole window: rows of Y; else rows of partial slot `slot` ([8, F], ld F)
-        float *const base = slot < 0 ? cj->Y + wrow * W * cj->ldy : cj->partial + (int64_t)slot * W * cj->F;
-        const int64_t ld = slot < 0 ? cj->ldy : cj->F;
+        float *const base = slot < 0 ? cj->Y + wrow * W * (int)cj->ldy : cj->partial + slot * W * F;
+        const int ld = slot < 0 ? (int)cj->ldy : F;
 #pragma unroll
         for (int t = 0; t < C::NT; ++t) {
             const int rl0 = t * 8 + 2 * tig;
 #pragma unroll
             for (int j = 0; j < C::MT; ++j) {
-                const int64_t fa = f0 + 16 * j + gid;
+                const int fa = f0 + 16 * j + gid;
 #pragma unroll
                 for (int h = 0; h < 4; ++h) {
                     const int rl = rl0 + (h & 1);
-                    const int64_t f = fa + (h >> 1) * 8;
-                    if (rl < W && wrow * W + rl < cj->m_out && f < cj->F) base[rl * ld + f] = acc[j][t][h];
+                    const int f = fa + (h >> 1) * 8;
+                    if (small && rl < W && wrow * W + rl < m_out && (full || f < F))
+                        base[rl * ld + f] = acc[j][t][h];
                     acc[j][t][h] = 0.f;
                 }
             }
@@ -1360,6 +1398,7 @@ __global__ void __launch_bounds__(256) k_reduce_groups_batched(const att_spmm_jo
     const int64_t n_jobs = header[0], n_r = header[3];
     for (int64_t gr = blockIdx.x; gr < n_r; gr += gridDim.x) {
         const att_spmm_job *j = jobs + find_prefix(jobs, n_jobs, gr, 2);
+        if (!job_small(j)) continue;  // skipped by the main pass (error bit 8)
         const int64_t k = gr - j->red_begin;
         const int g0 = __ldg(j->red_first + k);
         const int64_t w = __ldg(j->window_of_part + __ldg(j->group_part + g0));
@@ -1670,19 +1709,24 @@ int launch_fp8(const int32_t *rowptr, const int32_t *col, const void *val, const
                int64_t n_x, int64_t F, int64_t ldx, float *Y, int64_t m_out, int64_t ldy,
                int32_t *err, cudaStream_t st) {
     using C = CfgF8<W, FC>;
-    auto kernel = k_spmm_fp8<W, FC, WIDE>;
-    static std::once_flag once;
-    static int prep = ATT_OK;
-    std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
-    if (prep != ATT_OK) return prep;
     const int n_chunks = (int)((F + FC - 1) / FC);
     const int64_t items = n_parts * n_chunks;
     if (items == 0) return ATT_OK;
-    const int grid = occupancy_grid(kernel, C::SMEM, items);
-    kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const __half *)val, win, atomic,
-                                            n_parts, (const uint8_t *)X, xscale, n_x, F, ldx, Y,
-                                            m_out, ldy, n_chunks, err);
-    return launch_status("k_spmm_fp8");
+    const int64_t lim = INT32_MAX - (1 << 22);
+    const bool small = n_x * ldx < lim && m_out * ldy < lim && items < lim;
+    auto run = [&](auto kernel) {
+        static std::once_flag once;
+        static int prep = ATT_OK;
+        std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+        if (prep != ATT_OK) return prep;
+        const int grid = occupancy_grid(kernel, C::SMEM, items);
+        kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const __half *)val, win, atomic,
+                                                n_parts, (const uint8_t *)X, xscale, n_x, F, ldx,
+                                                Y, m_out, ldy, n_chunks, err);
+        return launch_status("k_spmm_fp8");
+    };
+    if (small) return run(k_spmm_fp8<W, FC, WIDE, int32_t>);
+    return run(k_spmm_fp8<W, FC, WIDE, int64_t>);
 }
 
 template <typename T, int W, int WIDE>

@@ -255,6 +255,10 @@ def build_job_table(jobs):
         if jb.groups.n_slots and (jb.partial is None or jb.partial.numel() < jb.groups.n_slots * 8 * F
                                   or jb.partial.dtype != torch.float32 or jb.partial.data_ptr() % 16):
             raise ValueError("partial buffer too small or misaligned for the job's multi-group windows")
+        lim = 2**31 - 4096
+        if (int(jb.X.shape[0]) * int(jb.X.stride(0)) >= lim or jb.m_out * int(jb.Y.stride(0)) >= lim
+                or jb.groups.n_slots * 8 * F >= lim):
+            raise ValueError("a batched job's element offsets must stay below 2^31")
         if jb.groups.m_out != jb.m_out:
             raise ValueError("groups were built for %d output rows, job has %d"
                              % (jb.groups.m_out, jb.m_out))

@@ -371,8 +371,12 @@ ATT_API size_t att_spmm_batched_grid(void);
  * multi-group windows, scratch (the work-queue counter, reset by the launch)}.
  * The launch reads the job count and sizes from device memory, so a captured
  * CUDA graph can be replayed after the table and header are rewritten.  Every
- * row < m_out of every Y is written.  err_flag (optional) gets bit 1 for a
- * column id outside [0, n_x), bit 2 for a part off the 8-column grid. */
+ * row < m_out of every Y is written.  Offsets are 32-bit: each job needs
+ * n_x * ldx, m_out * ldy and n_slots * 8 * F below 2^31 - 4096 and the total
+ * work items below 2^31 - grid * 4; a job that does not fit is skipped.
+ * err_flag (optional) gets bit 1 for a column id outside [0, n_x), bit 2 for
+ * a part off the 8-column grid, bit 8 for a job or item count that does not
+ * fit 32-bit offsets. */
 ATT_API int att_spmm_batched(const att_spmm_job *jobs, int64_t *header, int64_t grid,
                    int window, int wide, int32_t *err_flag, void *stream);
 
