@@ -114,7 +114,8 @@ struct GCfg {
 // PSPLIT: aggregate with P as a hi + lo pair of 16-bit values (fp32-accurate
 // output); the training path needs it so that dout . out matches the
 // backward's recomputed probabilities.
-template <typename T, int F, int MODE, bool PSPLIT>
+// IT: index type of items and element offsets (int32_t when every offset fits)
+template <typename T, int F, int MODE, bool PSPLIT, typename IT>
 __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     using C = GCfg<T, F, MODE>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -122,14 +123,15 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
     const unsigned char *sgen = smem + warp * C::WARP_SMEM;
     const int gid = lane >> 2, tig = lane & 3;
-    const int64_t n_items = A.n_chunks * A.H;
-    const int64_t stride = (int64_t)gridDim.x * kGWarps;
+    const IT n_items = (IT)(A.n_chunks * A.H);
+    const IT stride = (IT)gridDim.x * kGWarps;
+    const IT H = (IT)A.H, n_nodes = (IT)A.n_nodes, ldx = (IT)A.ldx, ldo = (IT)A.ldo;
     const T *X = (const T *)A.X;
     const float NEG_INF = -INFINITY;
 
     // ---- producer: (item, part, step) cursor ----
-    int64_t p_item = (int64_t)blockIdx.x * kGWarps + warp;
-    int64_t p_h = 0;
+    IT p_item = (IT)blockIdx.x * kGWarps + warp;
+    IT p_h = 0;
     int p_part = 0, p_part_end = 0, p_start = 0, p_nreal = 0, p_pend = 0, p_step = 0;
     int p_myc = -1;  // column ids of the producer's position, fetched one step ahead
     auto p_set_part = [&]() {  // returns with p_part < p_part_end and a non-empty part, or exhausted
@@ -149,16 +151,16 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             }
             p_item += stride;
             if (p_item >= n_items) return;
-            const int64_t ch = p_item / A.H;
-            p_h = p_item - ch * A.H;
+            const IT ch = p_item / H;
+            p_h = p_item - ch * H;
             p_part = A.chunk_begin[ch];
             p_part_end = A.chunk_begin[ch + 1];
         }
     };
     auto p_begin = [&]() {
         if (p_item < n_items) {
-            const int64_t ch = p_item / A.H;
-            p_h = p_item - ch * A.H;
+            const IT ch = p_item / H;
+            p_h = p_item - ch * H;
             p_part = A.chunk_begin[ch];
             p_part_end = A.chunk_begin[ch + 1];
             p_set_part();
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
         const uint32_t ss = ms + C::MSTAGE;
         const int c0 = p_step * 16;
         int myc = p_myc;
-        if (myc >= A.n_nodes || myc < -1) {
+        if ((uint64_t)(int64_t)(myc + 1) > (uint64_t)n_nodes) {  // valid: -1 .. n_nodes - 1
             if (A.err) atomicOr(A.err, 1);
             myc = -1;
         }
@@ -181,15 +183,15 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             const int cidx = __shfl_sync(0xffffffffu, myc, r & 15);
             if (idx < 16 * C::CPR) {
                 const bool ok = cidx >= 0;
-                const T *src = ok ? X + (int64_t)cidx * A.ldx + p_h * F + ch * 8 : X;
-                cp_async16(xs + r * C::XROW + ((ch ^ swz_row<F>(r)) << 4), src, ok ? 16 : 0);
+                const IT off = ok ? (IT)cidx * ldx + p_h * F + ch * 8 : (IT)0;
+                cp_async16(xs + r * C::XROW + ((ch ^ swz_row<F>(r)) << 4), X + off, ok ? 16 : 0);
             }
         }
         // occupancy bits of the step's 16 x 8 slots, one 8-byte piece per
         // 8-column half (a half past the part's padded end is zero-filled)
         if (lane < 2) {
             const bool ok = c0 + 8 * lane < p_pend - p_start;
-            const int64_t bit0 = (int64_t)(p_start + c0 + 8 * lane) * kW;
+            const IT bit0 = (IT)(p_start + c0 + 8 * lane) * kW;
             const uint32_t *src = ok ? A.mask + (bit0 >> 5) : A.mask;
             cp_async8(ms + 8 * lane, src, ok ? 8 : 0);
         }
@@ -197,7 +199,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             if (lane < 16) {
                 const int c = __shfl_sync(0x0000ffffu, myc, lane);
                 const bool ok = c >= 0;
-                cp_async4(ss + 4 * lane, ok ? (const void *)(A.s1 + p_h * A.n_nodes + c)
+                cp_async4(ss + 4 * lane, ok ? (const void *)(A.s1 + (p_h * n_nodes + c))
                                             : (const void *)A.s1,
                           ok ? 4 : 0);
             }
@@ -230,12 +232,12 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     }
 
     int cstage = 0, pstage = kGStages - 1;
-    for (int64_t c_item = (int64_t)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
-        const int64_t chunk = c_item / A.H;
-        const int64_t h = c_item - chunk * A.H;
+    for (IT c_item = (IT)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
+        const IT chunk = c_item / H;
+        const IT h = c_item - chunk * H;
         const int part0 = A.chunk_begin[chunk], part1 = A.chunk_begin[chunk + 1];
         if (part1 <= part0) continue;
-        const int64_t wrow = (int64_t)A.win[part0] * kW;
+        const IT wrow = (IT)A.win[part0] * kW;
         // query side of the window: B fragments (mode 0) or row scores (mode 1)
         uint32_t bq[C::MT][2];
         float s0r[2] = {0.f, 0.f};
@@ -244,17 +246,15 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             for (int kk = 0; kk < C::MT; ++kk)
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
-                    const int64_t row = wrow + gid;
+                    const IT row = wrow + gid;
                     const int f = 16 * kk + 2 * tig + 8 * u;
-                    bq[kk][u] = row < A.n_nodes
-                                    ? *(const uint32_t *)(X + row * A.ldx + h * F + f)
-                                    : 0u;
+                    bq[kk][u] = row < n_nodes ? *(const uint32_t *)(X + (row * ldx + h * F + f)) : 0u;
                 }
         } else {
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
-                const int64_t row = wrow + 2 * tig + u;
-                s0r[u] = row < A.n_nodes ? A.s0[h * A.n_nodes + row] : 0.f;
+                const IT row = wrow + 2 * tig + u;
+                s0r[u] = row < n_nodes ? A.s0[h * n_nodes + row] : 0.f;
             }
         }
         float m_run[2] = {NEG_INF, NEG_INF}, l_run[2] = {0.f, 0.f};
@@ -379,22 +379,22 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             for (int j = 0; j < C::MT; ++j)
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const int64_t row = wrow + 2 * tig + (u & 1);
+                    const IT row = wrow + 2 * tig + (u & 1);
                     const int f = 16 * j + gid + 8 * (u >> 1);
-                    if (row < A.n_nodes) A.out[row * A.ldo + h * F + f] = acc[j][u] * inv[u & 1];
+                    if (row < n_nodes) A.out[row * ldo + h * F + f] = acc[j][u] * inv[u & 1];
                 }
             if (gid == 0) {
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
-                    const int64_t row = wrow + 2 * tig + u;
-                    if (row < A.n_nodes) {
-                        if (A.row_max) A.row_max[h * A.n_nodes + row] = m_run[u];
-                        if (A.row_sum) A.row_sum[h * A.n_nodes + row] = l_run[u];
+                    const IT row = wrow + 2 * tig + u;
+                    if (row < n_nodes) {
+                        if (A.row_max) A.row_max[h * n_nodes + row] = m_run[u];
+                        if (A.row_sum) A.row_sum[h * n_nodes + row] = l_run[u];
                     }
                 }
             }
         } else {
-            float *pp = A.partial + ((int64_t)slot * A.H + h) * kW * (F + 2);
+            float *pp = A.partial + ((IT)slot * H + h) * kW * (F + 2);
 #pragma unroll
             for (int j = 0; j < C::MT; ++j)
 #pragma unroll
@@ -494,35 +494,44 @@ __global__ void k_slot_mask(const int32_t *__restrict__ edge_slot, int64_t nnz, 
 }
 
 template <typename T, int F, int MODE, bool PSPLIT>
-int run_gat(const GatArgs &P, cudaStream_t st) {
+int run_gat(const GatArgs &P, cudaStream_t st, int64_t n_partial) {
     using C = GCfg<T, F, MODE>;
-    auto kernel = k_gat_fused<T, F, MODE, PSPLIT>;
-    static std::once_flag once;
-    static int prep = ATT_OK;
-    std::call_once(once, [&] {
-        prep = cuda_status(
-            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
-            "cudaFuncSetAttribute");
-    });
-    if (prep != ATT_OK) return prep;
     const int64_t items = P.n_chunks * P.H;
     if (items == 0) return ATT_OK;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGThreads, C::SMEM);
-    if (per_sm < 1) per_sm = 1;
-    const int64_t want = (items + kGWarps - 1) / kGWarps;
-    const int64_t cap = (int64_t)sm_count() * per_sm;
-    kernel<<<(unsigned)(want < cap ? want : cap), kGThreads, C::SMEM, st>>>(P);
-    return launch_status("k_gat_fused");
+    // 32-bit offsets when X', the output, the statistics, the partials and
+    // the items all stay below 2^31 elements
+    const int64_t lim = INT32_MAX - (1 << 22);
+    const bool small = P.n_nodes * P.ldx < lim && P.n_nodes * P.ldo < lim &&
+                       P.H * P.n_nodes < lim && n_partial * P.H * kW * (P.F + 2) < lim &&
+                       items < lim;
+    auto run = [&](auto kernel) {
+        static std::once_flag once;
+        static int prep = ATT_OK;
+        std::call_once(once, [&] {
+            prep = cuda_status(
+                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
+                "cudaFuncSetAttribute");
+        });
+        if (prep != ATT_OK) return prep;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGThreads, C::SMEM);
+        if (per_sm < 1) per_sm = 1;
+        const int64_t want = (items + kGWarps - 1) / kGWarps;
+        const int64_t cap = (int64_t)sm_count() * per_sm;
+        kernel<<<(unsigned)(want < cap ? want : cap), kGThreads, C::SMEM, st>>>(P);
+        return launch_status("k_gat_fused");
+    };
+    if (small) return run(k_gat_fused<T, F, MODE, PSPLIT, int32_t>);
+    return run(k_gat_fused<T, F, MODE, PSPLIT, int64_t>);
 }
 
 template <typename T, int MODE>
-int dispatch_gat_f(const GatArgs &P, cudaStream_t st) {
+int dispatch_gat_f(const GatArgs &P, cudaStream_t st, int64_t np) {
     const bool split = P.row_sum != nullptr;  // statistics requested: training path
     switch (P.F) {
-        case 32: return split ? run_gat<T, 32, MODE, true>(P, st) : run_gat<T, 32, MODE, false>(P, st);
-        case 64: return split ? run_gat<T, 64, MODE, true>(P, st) : run_gat<T, 64, MODE, false>(P, st);
-        case 128: return split ? run_gat<T, 128, MODE, true>(P, st) : run_gat<T, 128, MODE, false>(P, st);
+        case 32: return split ? run_gat<T, 32, MODE, true>(P, st, np) : run_gat<T, 32, MODE, false>(P, st, np);
+        case 64: return split ? run_gat<T, 64, MODE, true>(P, st, np) : run_gat<T, 64, MODE, false>(P, st, np);
+        case 128: return split ? run_gat<T, 128, MODE, true>(P, st, np) : run_gat<T, 128, MODE, false>(P, st, np);
         default:
             set_error("fused GAT supports F in {32, 64, 128}, got %lld", (long long)P.F);
             return ATT_ERR_UNSUPPORTED;
@@ -905,8 +914,13 @@ extern "C" int att_gat_forward(const int32_t *rowptr, const int32_t *col, const 
               n_nodes, n_heads, F, ldx, mode, s0, s1, slope, out, ldo, row_max, row_sum, partial,
               err_flag};
     int s;
-    if (x_dtype == ATT_F16) s = mode == 0 ? dispatch_gat_f<__half, 0>(P, st) : dispatch_gat_f<__half, 1>(P, st);
-    else s = mode == 0 ? dispatch_gat_f<__nv_bfloat16, 0>(P, st) : dispatch_gat_f<__nv_bfloat16, 1>(P, st);
+    // partial slots are at most one per chunk
+    const int64_t np = P.n_chunks;
+    if (x_dtype == ATT_F16)
+        s = mode == 0 ? dispatch_gat_f<__half, 0>(P, st, np) : dispatch_gat_f<__half, 1>(P, st, np);
+    else
+        s = mode == 0 ? dispatch_gat_f<__nv_bfloat16, 0>(P, st, np)
+                      : dispatch_gat_f<__nv_bfloat16, 1>(P, st, np);
     if (s != ATT_OK) return s;
     if (n_multi > 0) {
         const int64_t threads = n_multi * n_heads * 32;
