@@ -39,6 +39,15 @@ sys.path.insert(0, ROOT)
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes per launch of the dominant kernel (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum, one launch after two, --clock-control none, GB300),
+# for the workload and scale they were measured on: a profiler counter cannot
+# be read inside the timed run, so the figure is carried here with its source.
+MEASURED_TRAFFIC = {
+    ("spmm_products_fp16", 1.0): {
+        "bytes": 9950022656 + 1406364928, "kernel": "k_spmm16<__half, 8, 64, 8, 3, int>",
+        "ncu_ms": 2.188, "note": "read 9.95 GB + write 1.41 GB; X rows of hub columns hit L2"},
+}
 METRIC = "SpMM/SDDMM HBM GB/s (% roofline); GAT step ms; serve p50/p99 vs plain"
 
 
@@ -993,8 +1002,13 @@ def main():
         base = None
         if not args.no_cpu_baseline:
             base = cpu_baseline(wl)
+        mt = MEASURED_TRAFFIC.get((wl.name, args.scale))
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                "frac": achieved / peak, "traffic": mt["bytes"] if mt else None,
+                "traffic_source": (dict(mt, method="ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                                   "one launch") if mt else None),
+                "dram_gbs_at_bench_time": (mt["bytes"] / (avg_launch_ms * 1e-3) / 1e9) if mt else None,
+                "peak_kind": peak_kind,
                 "kernel": getattr(wl, "kernel_name", "att_spmm (k_zero_uncovered + k_spmm16)")
                           + ", avg of %d launches" % args.steps,
                 "bytes_per_launch": kbytes}
