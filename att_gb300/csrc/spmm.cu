@@ -1105,6 +1105,238 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
 }
 
 // ---------------------------------------------------------------------------
+// FP8 E4M3 features dequantized in registers (values fp16)
+// ---------------------------------------------------------------------------
+// Same staging ring as k_spmm_fp8, without the fp16 tile: ldmatrix.trans
+// reads the e4m3 rows as 16-bit feature pairs, so each register holds
+// features (f, f+1) of two gathered rows (c, c+1).  One byte permute regroups
+// it into (f: c, c+1) | (f+1: c, c+1), two cvt.e4m3x2 -> f16x2 give the A
+// fragments of two MMA rows, and one multiply by the rows' scale pair applies
+// the per-row scales.  The MMA rows are thereby a permutation of the features
+// (row m < 8 is feature 2m of its 16-feature tile, row m + 8 is feature
+// 2m + 1), which the epilogue undoes: each lane ends up owning two adjacent
+// features of two window rows and stores them as float2.  This removes the
+// shared-memory round trip of the fp16 tile (4 KB of shared traffic and four
+// 16-byte stores per lane per step) and lets one work item cover 128 features.
+template <int W, int FC, int S = kF8Stages>
+struct CfgF8R {
+    static constexpr int XROW = FC;              // bytes per gathered e4m3 row
+    static constexpr int XSTAGE = 16 * XROW;
+    static constexpr int VSTAGE = 16 * W * 2;
+    static constexpr int SSTAGE = 64;            // 16 fp32 scales
+    static constexpr int STAGE = XSTAGE + VSTAGE + SSTAGE;
+    static constexpr int WARP_SMEM = S * STAGE;
+    static constexpr int SMEM = kWarps * WARP_SMEM;
+    static constexpr int CPR = FC / 16;          // 16-byte chunks per row
+    static constexpr int RPP = 32 / CPR;         // rows per warp pass
+    static constexpr int MT = FC / 16;           // 16-feature MMA tiles
+    static constexpr int NT = W / 8;
+    static constexpr int VCH = VSTAGE / 16;
+};
+
+__device__ __forceinline__ uint32_t hmul2_u32(uint32_t a, __half2 s) {
+    __half2 r = __hmul2(*reinterpret_cast<__half2 *>(&a), s);
+    return *reinterpret_cast<uint32_t *>(&r);
+}
+
+template <int W, int FC, int WIDE, typename IT>
+__global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
+    const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+    const __half *__restrict__ val, const int32_t *__restrict__ win,
+    const int32_t *__restrict__ atomic, int64_t n_parts, const uint8_t *__restrict__ X,
+    const float *__restrict__ xscale, int64_t n_x_, int64_t F_, int64_t ldx_, float *__restrict__ Y,
+    int64_t m_out_, int64_t ldy_, int n_chunks, int vec_out, int32_t *__restrict__ err) {
+    const IT n_x = (IT)n_x_, F = (IT)F_, ldx = (IT)ldx_, m_out = (IT)m_out_, ldy = (IT)ldy_;
+    using C = CfgF8R<W, FC>;
+    constexpr int S = kF8Stages;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
+    const unsigned char *sgen = smem + warp * C::WARP_SMEM;
+    const IT n_items = (IT)(n_parts * n_chunks);
+    const IT stride = (IT)gridDim.x * kWarps;
+    const int gid = lane >> 2, tig = lane & 3;
+
+    IT p_item = (IT)blockIdx.x * kWarps + warp;
+    int p_step = 0, p_fc = 0, p_myc = -1;
+    PartInfo p_pi = {0, 0, 0};
+    auto p_load = [&]() {
+        while (p_item < n_items) {
+            const IT part = p_item / n_chunks;
+            p_fc = (int)(p_item - part * n_chunks);
+            p_pi = part_info<WIDE>(rowptr, part, err);
+            p_step = 0;
+            if (p_pi.nsteps > 0) return;
+            p_item += stride;
+        }
+    };
+    auto issue = [&](int stage) {
+        const uint32_t xs = sbase + stage * C::STAGE;
+        const uint32_t vs = xs + C::XSTAGE;
+        const uint32_t ss = vs + C::VSTAGE;
+        const int c0 = p_step * 16;
+        int myc = p_myc;  // loaded one step ahead
+        if ((uint64_t)(int64_t)(myc + 1) > (uint64_t)n_x) {  // valid: -1 .. n_x - 1
+            if (err) atomicOr(err, 1);
+            myc = -1;
+        }
+        const IT fbase = (IT)p_fc * FC;
+        const bool full = fbase + FC <= F;
+#pragma unroll
+        for (int i = 0; i < 16 / C::RPP; ++i) {
+            const int r = i * C::RPP + lane / C::CPR;
+            const int ch = lane % C::CPR;
+            const int cidx = __shfl_sync(0xffffffffu, myc, r);
+            const IT f = fbase + ch * 16;
+            const bool ok = cidx >= 0 && (full || f < F);
+            const IT off = ok ? (IT)cidx * ldx + f : (IT)0;
+            cp_async16(xs + r * C::XROW + ((ch ^ swz<C::XROW>(r)) << 4), X + off, ok ? 16 : 0);
+        }
+#pragma unroll
+        for (int q = lane; q < C::VCH; q += 32) {
+            const int e = q * 8;
+            const int blk = e / (W * WIDE);
+            const bool ok = c0 + blk * WIDE < p_pi.nreal;
+            const __half *src = val + ((IT)(p_pi.start + c0) * W + e);
+            cp_async16(vs + q * 16, ok ? (const void *)src : (const void *)val, ok ? 16 : 0);
+        }
+        if (lane < 16) {
+            const bool ok = myc >= 0;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(ss + 4 * lane),
+                         "l"(ok ? xscale + myc : xscale), "r"(ok ? 4 : 0));
+        }
+    };
+    auto p_fetch = [&]() {
+        p_myc = -1;
+        if (p_item < n_items && p_step * 16 + (lane & 15) < p_pi.nreal)
+            p_myc = __ldg(col + p_pi.start + p_step * 16 + (lane & 15));
+    };
+    auto p_advance = [&]() {
+        if (++p_step >= p_pi.nsteps) {
+            p_item += stride;
+            p_load();
+        }
+        p_fetch();
+    };
+
+    p_load();
+    p_fetch();
+#pragma unroll
+    for (int s = 0; s < S - 1; ++s) {
+        if (p_item < n_items) {
+            issue(s);
+            p_advance();
+        }
+        cp_async_commit();
+    }
+
+    float acc[C::MT][C::NT][4];
+#pragma unroll
+    for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
+
+    // ldmatrix lane roles: matrix mi = lane / 8 holds gathered rows
+    // (mi / 2) * 8 + lane % 8 and 16-feature chunk (mi % 2) of a 32-feature pair
+    const int lm_k = ((lane >> 4) << 3) + (lane & 7);
+    const int lm_h = (lane >> 3) & 1;
+    int cstage = 0, pstage = S - 1;
+    for (IT c_item = (IT)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
+        const IT part = c_item / n_chunks;
+        const int fc = (int)(c_item - part * n_chunks);
+        const PartInfo pi = part_info<WIDE>(rowptr, part, nullptr);
+        for (int step = 0; step < pi.nsteps; ++step) {
+            cp_async_wait<S - 2>();
+            __syncwarp();
+            const uint32_t xs = sbase + cstage * C::STAGE;
+            const uint32_t vs = xs + C::XSTAGE;
+            const float *sc = (const float *)(sgen + cstage * C::STAGE + C::XSTAGE + C::VSTAGE);
+            // scale pairs of the gathered rows this lane's A fragments hold:
+            // rows (2 tig, 2 tig + 1) and (8 + 2 tig, 9 + 2 tig)
+            const float2 s_lo = *reinterpret_cast<const float2 *>(sc + 2 * tig);
+            const float2 s_hi = *reinterpret_cast<const float2 *>(sc + 8 + 2 * tig);
+            const __half2 h_lo = __floats2half2_rn(s_lo.x, s_lo.y);
+            const __half2 h_hi = __floats2half2_rn(s_hi.x, s_hi.y);
+            uint32_t b[C::NT][2];
+            {
+                const int q = lane >> 3, rr = lane & 7;
+                if constexpr (C::NT == 2) {
+                    const int kb = q & 1, r = (q >> 1) * 8 + rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x4(vs + e * 2, b[0][0], b[0][1], b[1][0], b[1][1]);
+                } else {
+                    const int kb = q & 1, r = rr;
+                    const int e = (kb * 8 / WIDE) * W * WIDE + r * WIDE + (kb * 8) % WIDE;
+                    ldsm_x2(vs + e * 2, b[0][0], b[0][1]);
+                }
+            }
+#pragma unroll
+            for (int jp = 0; jp < C::MT / 2; ++jp) {
+                const int ch = 2 * jp + lm_h;
+                uint32_t R[4];  // (rows 0-7 | 8-15) x (tile 2jp | 2jp+1)
+                ldsm_x4_trans(xs + lm_k * C::XROW + ((ch ^ swz<C::XROW>(lm_k)) << 4), R[0], R[1],
+                              R[2], R[3]);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    // bytes (f: c, f+1: c, f: c+1, f+1: c+1) -> (f: c, c+1 | f+1: c, c+1)
+                    const uint32_t p0 = __byte_perm(R[h], 0, 0x3120);      // rows 2tig, 2tig+1
+                    const uint32_t p1 = __byte_perm(R[h + 2], 0, 0x3120);  // rows 8+2tig, 9+2tig
+                    uint32_t a[4];
+                    a[0] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p0 & 0xffffu)), h_lo);
+                    a[1] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p0 >> 16)), h_lo);
+                    a[2] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p1 & 0xffffu)), h_hi);
+                    a[3] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p1 >> 16)), h_hi);
+#pragma unroll
+                    for (int t = 0; t < C::NT; ++t)
+                        mma_16816<__half>(acc[2 * jp + h][t], a, b[t][0], b[t][1]);
+                }
+            }
+            __syncwarp();
+            if (p_item < n_items) {
+                issue(pstage);
+                p_advance();
+            }
+            cp_async_commit();
+            cstage = cstage + 1 == S ? 0 : cstage + 1;
+            pstage = pstage + 1 == S ? 0 : pstage + 1;
+        }
+        // epilogue: tile j, lane -> features f0 + 16 j + 2 gid (+1), window
+        // rows t * 8 + 2 tig (+1); F is a multiple of 16, so both features of
+        // a pair are inside F together
+        const int wrow = __ldg(win + part);
+        const bool add = __ldg(atomic + part) != 0;
+        const IT f0 = (IT)fc * FC;
+#pragma unroll
+        for (int t = 0; t < C::NT; ++t) {
+            const IT r0 = (IT)wrow * W + t * 8 + 2 * tig;
+#pragma unroll
+            for (int j = 0; j < C::MT; ++j) {
+                const IT f = f0 + 16 * j + 2 * gid;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const IT r = r0 + h;
+                    const float v0 = acc[j][t][h], v1 = acc[j][t][h + 2];
+                    if (r < m_out && f < F) {
+                        float *dst = Y + (r * ldy + f);
+                        if (add) {
+                            red_add_f32(dst, v0);
+                            red_add_f32(dst + 1, v1);
+                        } else if (vec_out) {
+                            *reinterpret_cast<float2 *>(dst) = make_float2(v0, v1);
+                        } else {
+                            dst[0] = v0;
+                            dst[1] = v1;
+                        }
+                    }
+                    acc[j][t][h] = acc[j][t][h + 2] = 0.f;
+                }
+            }
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 // Batched SpMM over many graphs in one launch (the serving loop's kernel)
 // ---------------------------------------------------------------------------
 // The job table lives in device memory: a header {n_jobs, total items, total
@@ -1702,6 +1934,10 @@ int g_spmm_gather = 0;
 // (3.03 ms) beats 128 x 4 (4.24 ms) and 128 x 6 (5.92 ms).
 int g_spmm_stages = 3;
 int g_spmm_fc = 64;
+// FP8 kernel: 1 = A fragments dequantized in registers (k_spmm_fp8r, 128
+// features per item when F > 64), 0 = through an fp16 shared tile
+// (k_spmm_fp8); att_set_option("spmm_fp8", ...).
+int g_spmm_fp8 = 1;
 
 template <int W, int FC, int WIDE>
 int launch_fp8(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
@@ -1727,6 +1963,33 @@ int launch_fp8(const int32_t *rowptr, const int32_t *col, const void *val, const
     };
     if (small) return run(k_spmm_fp8<W, FC, WIDE, int32_t>);
     return run(k_spmm_fp8<W, FC, WIDE, int64_t>);
+}
+
+template <int W, int FC, int WIDE>
+int launch_fp8r(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
+                const int32_t *atomic, int64_t n_parts, const void *X, const float *xscale,
+                int64_t n_x, int64_t F, int64_t ldx, float *Y, int64_t m_out, int64_t ldy,
+                int32_t *err, cudaStream_t st) {
+    using C = CfgF8R<W, FC>;
+    const int n_chunks = (int)((F + FC - 1) / FC);
+    const int64_t items = n_parts * n_chunks;
+    if (items == 0) return ATT_OK;
+    const int64_t lim = INT32_MAX - (1 << 22);
+    const bool small = n_x * ldx < lim && m_out * ldy < lim && items < lim;
+    const int vec_out = (ldy % 2 == 0 && ((uintptr_t)Y & 7) == 0) ? 1 : 0;
+    auto run = [&](auto kernel) {
+        static std::once_flag once;
+        static int prep = ATT_OK;
+        std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
+        if (prep != ATT_OK) return prep;
+        const int grid = occupancy_grid(kernel, C::SMEM, items);
+        kernel<<<grid, kThreads, C::SMEM, st>>>(rowptr, col, (const __half *)val, win, atomic,
+                                                n_parts, (const uint8_t *)X, xscale, n_x, F, ldx,
+                                                Y, m_out, ldy, n_chunks, vec_out, err);
+        return launch_status("k_spmm_fp8r");
+    };
+    if (small) return run(k_spmm_fp8r<W, FC, WIDE, int32_t>);
+    return run(k_spmm_fp8r<W, FC, WIDE, int64_t>);
 }
 
 template <typename T, int W, int WIDE>
@@ -1859,6 +2122,20 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
                       ((uintptr_t)val & 15) == 0 && ldx >= F,
                   ATT_ERR_UNSUPPORTED,
                   "fp8 SpMM needs F and ldx multiples of 16 and 16-byte aligned X and values");
+#define ATT_F8R(Wv, FCv, WIDEv)                                                                \
+    return launch_fp8r<Wv, FCv, WIDEv>(rowptr, col, val, window_of_part, atomic, n_parts, X,   \
+                                       x_scale, n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st)
+        if (g_spmm_fp8 == 1) {
+            if (F > 64) {
+                if (window == 8) { if (wide == 8) ATT_F8R(8, 128, 8); ATT_F8R(8, 128, 16); }
+                if (wide == 8) ATT_F8R(16, 128, 8);
+                ATT_F8R(16, 128, 16);
+            }
+            if (window == 8) { if (wide == 8) ATT_F8R(8, 64, 8); ATT_F8R(8, 64, 16); }
+            if (wide == 8) ATT_F8R(16, 64, 8);
+            ATT_F8R(16, 64, 16);
+        }
+#undef ATT_F8R
 #define ATT_F8(Wv, FCv, WIDEv)                                                                \
     return launch_fp8<Wv, FCv, WIDEv>(rowptr, col, val, window_of_part, atomic, n_parts, X,   \
                                       x_scale, n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st)
@@ -1892,6 +2169,11 @@ extern "C" int att_set_option(const char *key, int value) {
         g_spmm_fc = value;
         return ATT_OK;
     }
+    if (strcmp(key, "spmm_fp8") == 0) {
+        ATT_CHECK(value == 0 || value == 1, ATT_ERR_INVALID, "spmm_fp8 must be 0 or 1");
+        g_spmm_fp8 = value;
+        return ATT_OK;
+    }
     set_error("unknown option '%s'", key);
     return ATT_ERR_INVALID;
 }
@@ -1905,6 +2187,10 @@ extern "C" int att_get_option(const char *key, int *value) {
     }
     if (strcmp(key, "spmm_stages") == 0) {
         *value = g_spmm_stages;
+        return ATT_OK;
+    }
+    if (strcmp(key, "spmm_fp8") == 0) {
+        *value = g_spmm_fp8;
         return ATT_OK;
     }
     if (strcmp(key, "spmm_fc") == 0) {

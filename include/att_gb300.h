@@ -66,7 +66,9 @@ enum att_dtype {
  *                  2 = one cp.async.bulk per gathered row (8-row windows,
  *                      8-wide blocks, 64-feature chunks).
  *   "spmm_stages": ring depth of the 16-bit cp.async kernel (2, 3, 4).
- *   "spmm_fc":     features per work item for F > 64 (64, the default, or 128). */
+ *   "spmm_fc":     features per work item for F > 64 (64, the default, or 128).
+ *   "spmm_fp8":    FP8 feature kernel: 1 = dequantized in registers (default),
+ *                  0 = dequantized through an fp16 shared-memory tile. */
 ATT_API int att_set_option(const char *key, int value);
 ATT_API int att_get_option(const char *key, int *value);
 

@@ -218,3 +218,69 @@ def test_bulk_row_copies_flag_bad_column(cuda, gather_mode):
     Y = ops.spmm(f.rowptr, col, f.val, f.window_of_part, f.atomic, X, 30, err_flag=err)
     torch.cuda.synchronize()
     assert int(err.item()) & 1 and bool(torch.isfinite(Y).all())
+
+
+@pytest.fixture
+def fp8_mode():
+    """Set att_set_option("spmm_fp8", mode) for a test and restore it."""
+    from att_gb300 import _lib
+    import ctypes
+    old = ctypes.c_int(1)
+    _lib.call("att_get_option", b"spmm_fp8", ctypes.byref(old))
+    yield lambda m: _lib.call("att_set_option", b"spmm_fp8", m)
+    _lib.call("att_set_option", b"spmm_fp8", old.value)
+
+
+@pytest.mark.parametrize("W,w", [(8, 8), (16, 8), (8, 16), (16, 16)])
+@pytest.mark.parametrize("F,pad", [(128, 0), (80, 0), (64, 0), (144, 0), (128, 1)])
+def test_fp8_register_dequant_matches_tile(cuda, fp8_mode, W, w, F, pad):
+    """The register-dequant FP8 kernel (spmm_fp8 = 1, the default) does the
+    tile kernel's arithmetic (the same fp16 products of code and scale, the
+    same fp32 accumulation order per part), so the two agree to fp32
+    rounding (split windows add atomically in any order).  Covers 128-feature
+    items with a partial last chunk (F = 80, 144), 64-feature items (F = 64),
+    an odd output stride (scalar stores instead of float2), split windows and
+    rows past the last window; and stays within 1e-2 of FP64 on the
+    dequantized features."""
+    from att_gb300 import graphs, ops
+    n = 2403
+    rowptr, col = graphs.random_csr(n, n, 20, seed=F + W + w, hub_rows=4, hub_len=1800,
+                                    empty_frac=0.2)
+    deg = np.full(n, 0.3, np.float16)
+    f = _format(rowptr, col, deg, W, w, 8)
+    assert int(f.atomic.sum()) > 0
+    X = torch.from_numpy(np.random.default_rng(F).uniform(-2, 2, (n, F)).astype(np.float32))
+    X[5] = 0  # an all-zero row: scale clamps, codes are zero
+    Xq, scale = _quant_e4m3(X)
+    m_out = n + 9
+    outs = []
+    for mode in (0, 1):
+        fp8_mode(mode)
+        Yb = torch.full((m_out, F + pad), float("nan"), device="cuda")
+        Y = Yb[:, :F]
+        ops.spmm(f.rowptr, f.col, f.val, f.window_of_part, f.atomic, Xq.cuda(), m_out, window=W,
+                 wide=w, x_scale=scale.cuda(), out=Y)
+        outs.append(Y.cpu().numpy())
+        if pad:
+            assert torch.isnan(Yb[:, F:]).all()
+    assert np.all(np.isfinite(outs[1]))
+    assert oracle.rel_err(outs[1], outs[0]) <= 1e-6
+    ev = oracle.gcn_values(rowptr, col, deg).astype(np.float64)
+    Xdq = (Xq.float() * scale[:, None]).double().numpy()
+    ref_q = _ref(rowptr, col, ev, Xdq, m_out, W)
+    assert oracle.rel_err(outs[1], ref_q) <= 1e-2
+    assert np.all(outs[1][n:] == 0)
+
+
+def test_fp8_register_dequant_flags_bad_column(cuda, fp8_mode):
+    from att_gb300 import ops
+    fp8_mode(1)
+    f = _format(ROW, COL, np.ones(32, np.float16), 8, 8, 32)
+    col = f.col.clone()
+    col[3] = 1000
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    Xq, scale = _quant_e4m3(torch.ones(30, 128))
+    Y = ops.spmm(f.rowptr, col, f.val, f.window_of_part, f.atomic, Xq.cuda(), 30,
+                 x_scale=scale.cuda(), err_flag=err)
+    torch.cuda.synchronize()
+    assert int(err.item()) & 1 and bool(torch.isfinite(Y).all())
