@@ -1766,24 +1766,33 @@ __global__ void k_empty_scatter(const int32_t *__restrict__ win, int64_t P, int6
 }
 
 // Zero the output rows that no unsplit part writes: rows of split windows,
-// of windows without parts and rows past the last window.  One warp per window.
+// of windows without parts and rows past the last window.  Each thread looks
+// up one window (binary search of the sorted window ids); the warp then zeroes
+// the windows that need it together, one row at a time across its lanes.
 __global__ void k_zero_uncovered(const int32_t *__restrict__ win, const int32_t *__restrict__ atomic,
                                  int64_t n_parts, int W, float *__restrict__ Y, int64_t m_out,
                                  int64_t F, int64_t ldy) {
     const int lane = threadIdx.x & 31;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t n_w = (m_out + W - 1) / W;
-    if (w >= n_w) return;
-    int64_t lo = 0, hi = n_parts;
-    while (lo < hi) {
-        int64_t mid = (lo + hi) >> 1;
-        if (__ldg(win + mid) < w) lo = mid + 1; else hi = mid;
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool need = false;
+    if (w < n_w) {
+        int64_t lo = 0, hi = n_parts;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (__ldg(win + mid) < w) lo = mid + 1; else hi = mid;
+        }
+        need = !(lo < n_parts && __ldg(win + lo) == w && __ldg(atomic + lo) == 0);
     }
-    const bool covered = lo < n_parts && __ldg(win + lo) == w && __ldg(atomic + lo) == 0;
-    if (covered) return;
-    const int64_t r1 = (w + 1) * W < m_out ? (w + 1) * W : m_out;
-    for (int64_t r = w * W; r < r1; ++r)
-        for (int64_t f = lane; f < F; f += 32) Y[r * ldy + f] = 0.f;
+    unsigned m = __ballot_sync(0xffffffffu, need);
+    while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1;
+        const int64_t ww = w - lane + l;
+        const int64_t r1 = (ww + 1) * W < m_out ? (ww + 1) * W : m_out;
+        for (int64_t r = ww * W; r < r1; ++r)
+            for (int64_t f = lane; f < F; f += 32) Y[r * ldy + f] = 0.f;
+    }
 }
 
 template <typename K>
@@ -2064,7 +2073,7 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
     if (m_out == 0 || F == 0) return ATT_OK;
     int s = ATT_OK;
     {
-        int64_t threads = (m_out + window - 1) / window * 32;
+        int64_t threads = (m_out + window - 1) / window;
         k_zero_uncovered<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
             window_of_part, atomic, n_parts, window, Y, m_out, F, ldy);
         s = launch_status("k_zero_uncovered");
