@@ -98,7 +98,8 @@ struct Cfg16 {
 // IT: index type of items and element offsets -- int32_t when every offset
 // into X, Y and the values fits (the common case: fewer instructions per
 // gathered row; the kernel is issue-bound), else int64_t.
-template <typename T, int W, int FC, int WIDE, int S, typename IT>
+// FULL: F is a multiple of FC (every chunk whole; no per-feature bounds checks)
+template <typename T, int W, int FC, int WIDE, int S, typename IT, bool FULL>
 __global__ void __launch_bounds__(kThreads, (Cfg16<T, W, FC, WIDE, S>::MINB)) k_spmm16(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
     const T *__restrict__ val, const int32_t *__restrict__ win,
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(kThreads, (Cfg16<T, W, FC, WIDE, S>::MINB)) k_
             myc = -1;
         }
         const IT fbase = (IT)p_fc * FC;
-        const bool full = fbase + FC <= F;  // the whole chunk is inside F (uniform)
+        const bool full = FULL || fbase + FC <= F;  // the whole chunk is inside F (uniform)
         // CPR lanes copy one row's FC features per pass (whole 128-byte lines
         // per instruction; spreading a row over lane pairs measured 2.4x
         // slower on the 2.45M-node graph)
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(kThreads, (Cfg16<T, W, FC, WIDE, S>::MINB)) k_
         const int wrow = __ldg(win + part);
         const bool add = __ldg(atomic + part) != 0;
         const IT f0 = (IT)fc * FC;
-        const bool full = f0 + FC <= F;
+        const bool full = FULL || f0 + FC <= F;
 #pragma unroll
         for (int t = 0; t < C::NT; ++t) {
             const IT r0 = (IT)wrow * W + t * 8 + 2 * tig;
@@ -1139,7 +1140,7 @@ __device__ __forceinline__ uint32_t hmul2_u32(uint32_t a, __half2 s) {
     return *reinterpret_cast<uint32_t *>(&r);
 }
 
-template <int W, int FC, int WIDE, typename IT>
+template <int W, int FC, int WIDE, typename IT, bool FULL>
 __global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
     const __half *__restrict__ val, const int32_t *__restrict__ win,
@@ -1181,7 +1182,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
             myc = -1;
         }
         const IT fbase = (IT)p_fc * FC;
-        const bool full = fbase + FC <= F;
+        const bool full = FULL || fbase + FC <= F;
 #pragma unroll
         for (int i = 0; i < 16 / C::RPP; ++i) {
             const int r = i * C::RPP + lane / C::CPR;
@@ -1316,7 +1317,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
                 for (int h = 0; h < 2; ++h) {
                     const IT r = r0 + h;
                     const float v0 = acc[j][t][h], v1 = acc[j][t][h + 2];
-                    if (r < m_out && f < F) {
+                    if (r < m_out && (FULL || f < F)) {
                         float *dst = Y + (r * ldy + f);
                         if (add) {
                             red_add_f32(dst, v0);
@@ -1836,8 +1837,9 @@ int launch16(const int32_t *rowptr, const int32_t *col, const void *val, const i
                                                 err);
         return launch_status("k_spmm16");
     };
-    if (small) return run(k_spmm16<T, W, FC, WIDE, S, int32_t>);
-    return run(k_spmm16<T, W, FC, WIDE, S, int64_t>);
+    if (small && F % FC == 0) return run(k_spmm16<T, W, FC, WIDE, S, int32_t, true>);
+    if (small) return run(k_spmm16<T, W, FC, WIDE, S, int32_t, false>);
+    return run(k_spmm16<T, W, FC, WIDE, S, int64_t, false>);
 }
 
 template <typename T, int S>
@@ -1997,8 +1999,9 @@ int launch_fp8r(const int32_t *rowptr, const int32_t *col, const void *val, cons
                                                 Y, m_out, ldy, n_chunks, vec_out, err);
         return launch_status("k_spmm_fp8r");
     };
-    if (small) return run(k_spmm_fp8r<W, FC, WIDE, int32_t>);
-    return run(k_spmm_fp8r<W, FC, WIDE, int64_t>);
+    if (small && F % FC == 0) return run(k_spmm_fp8r<W, FC, WIDE, int32_t, true>);
+    if (small) return run(k_spmm_fp8r<W, FC, WIDE, int32_t, false>);
+    return run(k_spmm_fp8r<W, FC, WIDE, int64_t, false>);
 }
 
 template <typename T, int W, int WIDE>

@@ -236,6 +236,8 @@ class SpmmProducts(PipelinedE2E):
             sx = 1
         self.bytes_alg = (4 * (n + 1) + self.nnz * (4 + 2) + self.U * F * sx + n * F * 4
                           + (self.U * 4 if self.x_kind == "fp8" else 0))
+        # the same pass with fp16 features: the yardstick for comparing forms
+        self.bytes_fp16 = 4 * (n + 1) + self.nnz * (4 + 2) + self.U * F * 2 + n * F * 4
         self.flops = 2 * self.nnz * F
         self.launches_per_step = 2  # k_zero_uncovered + k_spmm16
         self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz,
@@ -575,6 +577,7 @@ class SpmmProductsFP8(SpmmProducts):
     name = "spmm_products_fp8"
     e2e_api = "att_gb300.ops.spmm (C ABI att_spmm), fp8 e4m3 + row scales"
     x_kind = "fp8"
+    kernel_name = "att_spmm (k_zero_uncovered + k_spmm_fp8r)"
 
 
 WORKLOADS = {SpmmProducts.name: SpmmProducts, GatReddit.name: GatReddit,
@@ -1083,6 +1086,8 @@ def main():
                 "clocks": clocks,
                 "gflops": world * wl.flops / (ms_per_step * 1e-3) / 1e9,
                 "plain_dropin_ms_per_step": plain_ms,
+                "fp16_equivalent_gbs": (world * wl.bytes_fp16 / (ms_per_step * 1e-3) / 1e9
+                                        if hasattr(wl, "bytes_fp16") else None),
                 "check_rel_err": check_err,
                 "err_vs_fp64": getattr(wl, "err_vs_fp64", None),
                 "launch_ms_p50": per_launch[len(per_launch) // 2]}
