@@ -231,6 +231,15 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
         cp_async_commit();
     }
 
+    // occupancy-bit positions of this lane's four (column, row) slots within
+    // a step's 16 x 8 block run: fixed per lane (wide is a power of two)
+    const int wmask = A.wide - 1;
+    int mbit[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int c = gid + 8 * (u >> 1), r = 2 * tig + (u & 1);
+        mbit[u] = (c & ~wmask) * kW + r * A.wide + (c & wmask);
+    }
     int cstage = 0, pstage = kGStages - 1;
     for (IT c_item = (IT)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
         const IT chunk = c_item / H;
@@ -267,7 +276,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             const int e = A.rowptr[2 * part + 1];
             const int pend = A.rowptr[2 * part + 2];
             int nreal = e > start ? e - start : 0;
-            if ((start % A.wide) != 0 || (pend % A.wide) != 0 || pend < start + nreal) nreal = 0;
+            if ((start & wmask) != 0 || (pend & wmask) != 0 || pend < start + nreal) nreal = 0;
             const int nsteps = (nreal + 15) >> 4;
             for (int step = 0; step < nsteps; ++step) {
                 cp_async_wait<kGStages - 2>();
@@ -301,9 +310,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int c = gid + 8 * (u >> 1);
-                    const int r = 2 * tig + (u & 1);
-                    const int bit = (c - c % A.wide) * kW + r * A.wide + c % A.wide;
-                    const bool occ = c0 + c < nreal && ((mw[bit >> 5] >> (bit & 31)) & 1u);
+                    const bool occ = c0 + c < nreal && ((mw[mbit[u] >> 5] >> (mbit[u] & 31)) & 1u);
                     const float x = sv[u];
                     sv[u] = occ ? (x > 0.f ? x : A.slope * x) : NEG_INF;
                 }
@@ -333,12 +340,16 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                 }
                 l_run[0] = l_run[0] * alpha[0] + ps[0];
                 l_run[1] = l_run[1] * alpha[1] + ps[1];
+                // rescale only when some row's max moved (rare after a window's
+                // first steps); alpha is exactly 1 otherwise
+                if (__any_sync(0xffffffffu, alpha[0] != 1.f || alpha[1] != 1.f)) {
 #pragma unroll
-                for (int j = 0; j < C::MT; ++j) {
-                    acc[j][0] *= alpha[0];
-                    acc[j][1] *= alpha[1];
-                    acc[j][2] *= alpha[0];
-                    acc[j][3] *= alpha[1];
+                    for (int j = 0; j < C::MT; ++j) {
+                        acc[j][0] *= alpha[0];
+                        acc[j][1] *= alpha[1];
+                        acc[j][2] *= alpha[0];
+                        acc[j][3] *= alpha[1];
+                    }
                 }
                 // P^T into B fragments: (col gid, rows 2tig..) -> (row gid, cols 2tig..)
                 const uint32_t h01 = pack2<T>(p[0], p[1]), h23 = pack2<T>(p[2], p[3]);
@@ -680,6 +691,13 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         cp_async_commit();
     }
 
+    const int wmask = A.wide - 1;  // wide is a power of two
+    int mbit[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int c = gid + 8 * (u >> 1), r = 2 * tig + (u & 1);
+        mbit[u] = (c & ~wmask) * kW + r * A.wide + (c & wmask);
+    }
     int cstage = 0, pstage = kGStages - 1;
     for (int64_t c_item = (int64_t)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
         const int64_t part = c_item / A.H;
@@ -688,7 +706,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         const int e = A.rowptr[2 * part + 1];
         const int pend = A.rowptr[2 * part + 2];
         int nreal = e > start ? e - start : 0;
-        if ((start % A.wide) != 0 || (pend % A.wide) != 0 || pend < start + nreal) nreal = 0;
+        if ((start & wmask) != 0 || (pend & wmask) != 0 || pend < start + nreal) nreal = 0;
         const int nsteps = (nreal + 15) >> 4;
         if (nsteps == 0) continue;
         const int64_t wrow = (int64_t)A.win[part] * kW;
@@ -739,9 +757,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int c = gid + 8 * (u >> 1);
-                const int r = 2 * tig + (u & 1);
-                const int bit = (c - c % A.wide) * kW + r * A.wide + c % A.wide;
-                const bool occ = c0 + c < nreal && ((mw[bit >> 5] >> (bit & 31)) & 1u);
+                const bool occ = c0 + c < nreal && ((mw[mbit[u] >> 5] >> (mbit[u] & 31)) & 1u);
                 const float s0c = cv[c], mc = cv[16 + c], lc = cv[32 + c], cc = cv[48 + c];
                 const float z = s0c + s1r[u & 1];
                 const float lr = z > 0.f ? z : A.slope * z;
