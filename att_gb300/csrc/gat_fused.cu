@@ -586,7 +586,7 @@ struct BCfg {
     static constexpr int TILE = 16 * XROW;
     static constexpr int XSTAGE = (SPLIT ? 2 : 1) * TILE;
     static constexpr int MSTAGE = 16;
-    static constexpr int CSTAGE = 4 * 64;  // s0, m, l, c of the 16 columns
+    static constexpr int CSTAGE = 5 * 64;  // s0, m, l, c and the ids of the 16 columns
     static constexpr int STAGE = XSTAGE + MSTAGE + CSTAGE;
     static constexpr int WARP_SMEM = kGStages * STAGE;
     static constexpr int SMEM = kGWarps * WARP_SMEM;
@@ -665,6 +665,9 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
 #pragma unroll
             for (int a = 0; a < 4; ++a)
                 cp_async4(cs + a * 64 + 4 * lane, arrs[a] + o, ok ? 4 : 0);
+            // the column ids themselves, for the ds0 scatter (-1: none)
+            asm volatile("st.shared.u32 [%0], %1;\n" ::"r"(cs + 4 * 64 + 4 * lane), "r"(myc)
+                         : "memory");
         }
     };
     auto p_fetch = [&]() {
@@ -761,7 +764,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
                 const float s0c = cv[c], mc = cv[16 + c], lc = cv[32 + c], cc = cv[48 + c];
                 const float z = s0c + s1r[u & 1];
                 const float lr = z > 0.f ? z : A.slope * z;
-                const float pv = occ && lc > 0.f ? __expf(lr - mc) / lc : 0.f;
+                const float pv = occ && lc > 0.f ? __fdividef(__expf(lr - mc), lc) : 0.f;
                 p[u] = pv;
                 dz[u] = pv * (dp[u] - cc) * (z > 0.f ? 1.f : A.slope);
             }
@@ -784,12 +787,9 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
             if (tig == 0) {
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
-                    const int c = gid + 8 * u;
-                    if (c0 + c < nreal) {
-                        const int ci = A.col[start + c0 + c];
-                        if (ci >= 0 && ci < A.n_nodes)
-                            red_add_f32(A.ds0 + h * A.n_nodes + ci, u ? c_hi : c_lo);
-                    }
+                    const int ci = ((const int *)(cv + 64))[gid + 8 * u];  // -1 past nreal
+                    if (ci >= 0 && ci < A.n_nodes)
+                        red_add_f32(A.ds0 + h * A.n_nodes + ci, u ? c_hi : c_lo);
                 }
             }
             // dX'_r += sum_c p[c][r] dout_c
@@ -975,4 +975,145 @@ extern "C" int att_gat_backward(const int32_t *rowptr_t, const int32_t *col_t,
                  ds0, ds1, err_flag};
     cudaStream_t st = (cudaStream_t)stream;
     return x_dtype == ATT_F16 ? dispatch_gat_bwd<__half>(P, st) : dispatch_gat_bwd<__nv_bfloat16>(P, st);
+}
+
+// ---------------------------------------------------------------------------
+// Elementwise ends of the fused GAT backward (one pass each over [N, H*F])
+// ---------------------------------------------------------------------------
+namespace att {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T to_t(float v);
+template <>
+__device__ __forceinline__ __half to_t<__half>(float v) { return __float2half_rn(v); }
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_t<__nv_bfloat16>(float v) {
+    return __float2bfloat16_rn(v);
+}
+template <typename T>
+__device__ __forceinline__ float from_t(T v);
+template <>
+__device__ __forceinline__ float from_t<__half>(__half v) { return __half2float(v); }
+template <>
+__device__ __forceinline__ float from_t<__nv_bfloat16>(__nv_bfloat16 v) {
+    return __bfloat162float(v);
+}
+
+// One warp per node row: c[h][n] = dout[n, h] . out[n, h] (fp32), and dout
+// split into a 16-bit hi part and the 16-bit rounding of its remainder.
+template <typename T>
+__global__ void k_gat_grad_prepare(const float *__restrict__ dout, int64_t ldd,
+                                   const float *__restrict__ out, int64_t ldo, int64_t n_nodes,
+                                   int64_t H, int64_t F, T *__restrict__ hi, T *__restrict__ lo,
+                                   int64_t ldh, float *__restrict__ c) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (n >= n_nodes) return;
+    for (int64_t h = 0; h < H; ++h) {
+        float s = 0.f;
+        for (int64_t f = lane; f < F; f += 32) {
+            const int64_t col = h * F + f;
+            const float d = dout[n * ldd + col];
+            s += d * out[n * ldo + col];
+            const T dh = to_t<T>(d);
+            hi[n * ldh + col] = dh;
+            lo[n * ldh + col] = to_t<T>(d - from_t<T>(dh));
+        }
+        s = warp_sum(s);
+        if (lane == 0) c[h * n_nodes + n] = s;
+    }
+}
+
+// dX[n, hF+f] = cast(dXp[n, hF+f] + ds0[h][n] a0[h][f] + ds1[h][n] a1[h][f]);
+// da0[h][f] += sum_n ds0[h][n] X'[n, hF+f], da1 likewise (fp32 atomics, one
+// per column per thread).  A block covers 256 columns of several rows per
+// sweep (256 / HF rows when HF <= 256).
+template <typename T>
+__global__ void __launch_bounds__(256) k_gat_grad_finish(
+    const float *__restrict__ dXp, int64_t ldg, const float *__restrict__ ds0,
+    const float *__restrict__ ds1, const float *__restrict__ a0, const float *__restrict__ a1,
+    const T *__restrict__ Xp, int64_t ldx, int64_t n_nodes, int64_t H, int64_t F,
+    T *__restrict__ dX, int64_t ldo, float *__restrict__ da0, float *__restrict__ da1) {
+    const int64_t HF = H * F;
+    const int t = threadIdx.x;
+    const int64_t cols = HF < 256 ? HF : 256;
+    const int64_t rows = 256 / cols;  // rows per sweep of the block
+    const int64_t roff = t / cols;
+    if (roff >= rows) return;
+    for (int64_t cb = 0; cb < HF; cb += 256) {
+        const int64_t col = cb + t % cols;
+        if (col >= HF) continue;
+        const int64_t h = col / F;
+        const float w0 = a0[col], w1 = a1[col];
+        float acc0 = 0.f, acc1 = 0.f;
+        for (int64_t n = (int64_t)blockIdx.x * rows + roff; n < n_nodes; n += (int64_t)gridDim.x * rows) {
+            const float g0 = ds0[h * n_nodes + n], g1 = ds1[h * n_nodes + n];
+            const float x = from_t<T>(Xp[n * ldx + col]);
+            dX[n * ldo + col] = to_t<T>(dXp[n * ldg + col] + g0 * w0 + g1 * w1);
+            acc0 += g0 * x;
+            acc1 += g1 * x;
+        }
+        atomicAdd(da0 + col, acc0);
+        atomicAdd(da1 + col, acc1);
+    }
+}
+
+}  // namespace
+}  // namespace att
+
+extern "C" int att_gat_grad_prepare(const float *dout, int64_t ldd, const float *out, int64_t ldo,
+                                    int64_t n_nodes, int64_t n_heads, int64_t F, void *dout_hi,
+                                    void *dout_lo, int dtype, int64_t ldh, float *c, void *stream) {
+    using namespace att;
+    clear_error();
+    ATT_CHECK(dtype == ATT_F16 || dtype == ATT_BF16, ATT_ERR_UNSUPPORTED,
+              "dout splits into fp16 or bf16");
+    ATT_CHECK(n_nodes >= 0 && n_heads > 0 && F > 0, ATT_ERR_INVALID, "bad sizes");
+    ATT_CHECK(ldd >= n_heads * F && ldo >= n_heads * F && ldh >= n_heads * F, ATT_ERR_INVALID,
+              "row strides shorter than heads x F");
+    if (n_nodes == 0) return ATT_OK;
+    ATT_CHECK(dout && out && dout_hi && dout_lo && c, ATT_ERR_INVALID, "null pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t threads = n_nodes * 32;
+    const unsigned grid = (unsigned)((threads + 255) / 256);
+    if (dtype == ATT_F16)
+        k_gat_grad_prepare<__half><<<grid, 256, 0, st>>>(dout, ldd, out, ldo, n_nodes, n_heads, F,
+                                                         (__half *)dout_hi, (__half *)dout_lo, ldh, c);
+    else
+        k_gat_grad_prepare<__nv_bfloat16><<<grid, 256, 0, st>>>(
+            dout, ldd, out, ldo, n_nodes, n_heads, F, (__nv_bfloat16 *)dout_hi,
+            (__nv_bfloat16 *)dout_lo, ldh, c);
+    return launch_status("k_gat_grad_prepare");
+}
+
+extern "C" int att_gat_grad_finish(const float *dXp, int64_t ldg, const float *ds0, const float *ds1,
+                                   const float *a0, const float *a1, const void *Xp, int dtype,
+                                   int64_t ldx, int64_t n_nodes, int64_t n_heads, int64_t F, void *dX,
+                                   int64_t ld_dx, float *da0, float *da1, void *stream) {
+    using namespace att;
+    clear_error();
+    ATT_CHECK(dtype == ATT_F16 || dtype == ATT_BF16, ATT_ERR_UNSUPPORTED,
+              "X' and dX are fp16 or bf16");
+    ATT_CHECK(n_nodes >= 0 && n_heads > 0 && F > 0, ATT_ERR_INVALID, "bad sizes");
+    ATT_CHECK(ldg >= n_heads * F && ldx >= n_heads * F && ld_dx >= n_heads * F, ATT_ERR_INVALID,
+              "row strides shorter than heads x F");
+    if (n_nodes == 0) return ATT_OK;
+    ATT_CHECK(dXp && ds0 && ds1 && a0 && a1 && Xp && dX && da0 && da1, ATT_ERR_INVALID,
+              "null pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t HF = n_heads * F;
+    const int64_t rows = 256 / (HF < 256 ? HF : 256);
+    int64_t want = (n_nodes + rows - 1) / rows;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    const unsigned grid = (unsigned)(want < cap ? want : cap);
+    if (dtype == ATT_F16)
+        k_gat_grad_finish<__half><<<grid, 256, 0, st>>>(dXp, ldg, ds0, ds1, a0, a1,
+                                                        (const __half *)Xp, ldx, n_nodes, n_heads,
+                                                        F, (__half *)dX, ld_dx, da0, da1);
+    else
+        k_gat_grad_finish<__nv_bfloat16><<<grid, 256, 0, st>>>(
+            dXp, ldg, ds0, ds1, a0, a1, (const __nv_bfloat16 *)Xp, ldx, n_nodes, n_heads, F,
+            (__nv_bfloat16 *)dX, ld_dx, da0, da1);
+    return launch_status("k_gat_grad_finish");
 }

@@ -69,15 +69,22 @@ class GATGraph:
         [n_nodes, H*F], ds0, ds1 fp32 [H, n_nodes]) with
         dXp_agg[j] = sum_i p_ij dout_i and ds0 / ds1 the gradients of the
         scores s0 / s1.  ``c[h][i] = dout_i . out_i``."""
+        dout32 = dout.float()
+        hi = dout32.to(Xp.dtype).contiguous()
+        lo = (dout32 - hi.float()).to(Xp.dtype).contiguous()
+        return self.attention_backward_split(Xp, hi, lo, s0, s1, row_max, row_sum, c, n_heads,
+                                             slope)
+
+    def attention_backward_split(self, Xp, dout, dout_lo, s0, s1, row_max, row_sum, c, n_heads,
+                                 slope=0.2):
+        """attention_backward with dout given as its 16-bit hi part and the
+        16-bit rounding of the remainder (att_gat_grad_prepare makes both)."""
         require_cuda()
         T = self.transposed()
         f = T.fmt
         N = self.n_nodes
         F = Xp.shape[1] // n_heads
         Xp = Xp.contiguous()
-        dout32 = dout.float()
-        dout = dout32.to(Xp.dtype).contiguous()
-        dout_lo = (dout32 - dout.float()).to(Xp.dtype).contiguous()
         dXp = torch.zeros(N, n_heads * F, dtype=torch.float32, device=Xp.device)
         ds0 = torch.zeros(n_heads, N, dtype=torch.float32, device=Xp.device)
         ds1 = torch.zeros(n_heads, N, dtype=torch.float32, device=Xp.device)
@@ -184,15 +191,25 @@ class GATAttention(torch.autograd.Function):
         G, H, slope = ctx.graph, ctx.n_heads, ctx.slope
         N = G.n_nodes
         F = Xp.shape[1] // H
-        dout = dout.contiguous()
-        c = (dout.view(N, H, F) * out.view(N, H, F)).sum(-1).t().contiguous()
-        dXp, ds0, ds1 = G.attention_backward(Xp, dout, s0, s1, rmax, rsum, c, H, slope)
-        X3 = Xp.view(N, H, F).float()
-        dX3 = dXp.view(N, H, F) + ds0.t()[:, :, None] * a0.float()[None] + \
-            ds1.t()[:, :, None] * a1.float()[None]
-        da0 = torch.einsum("hn,nhf->hf", ds0, X3).to(a0.dtype)
-        da1 = torch.einsum("hn,nhf->hf", ds1, X3).to(a1.dtype)
-        return dX3.reshape(N, H * F).to(Xp.dtype), da0, da1, None, None, None
+        dev = Xp.device
+        dout = dout.float().contiguous()
+        out = out.contiguous()
+        # c[h][i] = dout_i . out_i and the hi/lo split of dout, one pass
+        hi = torch.empty(N, H * F, dtype=Xp.dtype, device=dev)
+        lo = torch.empty_like(hi)
+        c = torch.empty(H, N, dtype=torch.float32, device=dev)
+        _lib.call("att_gat_grad_prepare", _p(dout), dout.stride(0), _p(out), out.stride(0), N, H,
+                  F, _p(hi), _p(lo), _DT[Xp.dtype], hi.stride(0), _p(c), _stream())
+        dXp, ds0, ds1 = G.attention_backward_split(Xp, hi, lo, s0, s1, rmax, rsum, c, H, slope)
+        # dX' = dXp + ds0 a0 + ds1 a1 (cast to X' dtype), da0 / da1 = sum_n ds X', one pass
+        Xp = Xp.contiguous()
+        dX = torch.empty(N, H * F, dtype=Xp.dtype, device=dev)
+        da0 = torch.zeros(H, F, dtype=torch.float32, device=dev)
+        da1 = torch.zeros(H, F, dtype=torch.float32, device=dev)
+        _lib.call("att_gat_grad_finish", _p(dXp), dXp.stride(0), _p(ds0), _p(ds1),
+                  _p(a0.float().contiguous()), _p(a1.float().contiguous()), _p(Xp), _DT[Xp.dtype],
+                  Xp.stride(0), N, H, F, _p(dX), dX.stride(0), _p(da0), _p(da1), _stream())
+        return dX, da0.to(a0.dtype), da1.to(a1.dtype), None, None, None
 
 
 class GATConv(torch.nn.Module):

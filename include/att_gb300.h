@@ -317,6 +317,24 @@ ATT_API int att_gat_backward(const int32_t *rowptr_t, const int32_t *col_t,
                    const float *row_sum, const float *c, float slope, float *dXp, int64_t ldg,
                    float *ds0, float *ds1, int32_t *err_flag, void *stream);
 
+/* The elementwise ends of the fused GAT backward, one pass over [N, H*F]
+ * each (no counterpart in the reference, whose backward does them as separate
+ * torch ops between its extension calls:
+ * end2end_ori/gat_final/mgat_csr/mgat_conv.py:34-151).
+ *   att_gat_grad_prepare: c[h][n] = dout[n, hF:hF+F] . out[n, hF:hF+F] (fp32)
+ *     and dout split into dout_hi = dtype(dout), dout_lo = dtype(dout - hi),
+ *     the inputs att_gat_backward takes.
+ *   att_gat_grad_finish: dX[n, hF+f] = dtype(dXp + ds0[h][n] a0[h][f] +
+ *     ds1[h][n] a1[h][f]), and da0[h][f] += sum_n ds0[h][n] Xp[n, hF+f], da1
+ *     likewise (fp32 atomics: zero da0 / da1 first).  dtype: fp16 or bf16. */
+ATT_API int att_gat_grad_prepare(const float *dout, int64_t ldd, const float *out, int64_t ldo,
+                   int64_t n_nodes, int64_t n_heads, int64_t F, void *dout_hi, void *dout_lo,
+                   int dtype, int64_t ldh, float *c, void *stream);
+ATT_API int att_gat_grad_finish(const float *dXp, int64_t ldg, const float *ds0, const float *ds1,
+                   const float *a0, const float *a1, const void *Xp, int dtype, int64_t ldx,
+                   int64_t n_nodes, int64_t n_heads, int64_t F, void *dX, int64_t ld_dx,
+                   float *da0, float *da1, void *stream);
+
 /* ======================================================================
  * Batched SpMM over many graphs in one launch (the serving loop's kernel; no
  * counterpart in the reference, which runs one graph per call).

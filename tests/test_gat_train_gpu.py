@@ -82,3 +82,54 @@ def test_backward_matches_fp64_finite_differences(cuda):
         an = float((grads[which] * v[which]).sum())
         ra = float((refg[which] * v[which]).sum())
         assert abs(an - fd) <= 1e-2 * max(abs(fd), 1.0), (which, an, fd, ra)
+
+
+@pytest.mark.parametrize("H,F,dtype", [(1, 40, torch.bfloat16), (4, 64, torch.bfloat16),
+                                       (5, 64, torch.float16), (3, 24, torch.float16)])
+def test_grad_prepare_and_finish_kernels(cuda, H, F, dtype):
+    """att_gat_grad_prepare / att_gat_grad_finish through the C ABI against
+    their definitions in FP64: c = dout . out per head, dout = hi + lo (hi the
+    16-bit rounding, lo the rounding of the remainder), dX = dtype(dXp + ds0 a0
+    + ds1 a1) and da0/da1 = sum_n ds X'.  Covers H*F below, at and above the
+    256-column block (40, 256, 320) and one that does not divide it (72)."""
+    from att_gb300 import _lib
+    from att_gb300.ops import _DT, _p, _stream
+    n = 3001
+    g = torch.Generator().manual_seed(H * 100 + F)
+    HF = H * F
+    dout = torch.randn(n, HF, generator=g).cuda()
+    out = torch.randn(n, HF, generator=g).cuda()
+    hi = torch.empty(n, HF, dtype=dtype, device="cuda")
+    lo = torch.empty_like(hi)
+    c = torch.full((H, n), float("nan"), device="cuda")
+    _lib.call("att_gat_grad_prepare", _p(dout), HF, _p(out), HF, n, H, F, _p(hi), _p(lo),
+              _DT[dtype], HF, _p(c), _stream())
+    torch.cuda.synchronize()
+    c_ref = (dout.double().view(n, H, F) * out.double().view(n, H, F)).sum(-1).t()
+    assert oracle.rel_err(c.cpu().numpy(), c_ref.cpu().numpy()) <= 1e-6
+    assert torch.equal(hi, dout.to(dtype))
+    assert torch.equal(lo, (dout - dout.to(dtype).float()).to(dtype))
+    # finish
+    dXp = torch.randn(n, HF, generator=g).cuda()
+    ds0 = torch.randn(H, n, generator=g).cuda()
+    ds1 = torch.randn(H, n, generator=g).cuda()
+    a0 = torch.randn(H, F, generator=g).cuda()
+    a1 = torch.randn(H, F, generator=g).cuda()
+    Xp = torch.randn(n, HF, generator=g).to(dtype).cuda()
+    dX = torch.empty(n, HF, dtype=dtype, device="cuda")
+    da0 = torch.zeros(H, F, device="cuda")
+    da1 = torch.zeros(H, F, device="cuda")
+    _lib.call("att_gat_grad_finish", _p(dXp), HF, _p(ds0), _p(ds1), _p(a0), _p(a1), _p(Xp),
+              _DT[dtype], HF, n, H, F, _p(dX), HF, _p(da0), _p(da1), _stream())
+    torch.cuda.synchronize()
+    X3 = Xp.double().view(n, H, F)
+    dX_ref = (dXp.double().view(n, H, F) + ds0.double().t()[:, :, None] * a0.double()[None]
+              + ds1.double().t()[:, :, None] * a1.double()[None]).reshape(n, HF)
+    # one rounding to the 16-bit type: within its half-ulp (2^-8 bf16, 2^-11 fp16) relative
+    tol = 2.0 ** -8 if dtype == torch.bfloat16 else 2.0 ** -11
+    d = (dX.double() - dX_ref).abs() <= tol * dX_ref.abs() + 1e-6
+    assert bool(d.all())
+    da0_ref = torch.einsum("hn,nhf->hf", ds0.double(), X3)
+    da1_ref = torch.einsum("hn,nhf->hf", ds1.double(), X3)
+    assert oracle.rel_err(da0.cpu().numpy(), da0_ref.cpu().numpy()) <= 1e-5
+    assert oracle.rel_err(da1.cpu().numpy(), da1_ref.cpu().numpy()) <= 1e-5
