@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
         // 8-column half (a half past the part's padded end is zero-filled)
         if (lane < 2) {
             const bool ok = c0 + 8 * lane < p_pend - p_start;
-            const IT bit0 = (IT)(p_start + c0 + 8 * lane) * kW;
+            const int64_t bit0 = (int64_t)(p_start + c0 + 8 * lane) * kW;  // bit index: 64-bit always
             const uint32_t *src = ok ? A.mask + (bit0 >> 5) : A.mask;
             cp_async8(ms + 8 * lane, src, ok ? 8 : 0);
         }
@@ -427,49 +427,48 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     cp_async_wait<0>();
 }
 
-// Merge the partials of windows spread over several chunks: one warp per
-// (window, head); the window's chunks are [multi[2i], multi[2i+1]).
-__global__ void k_gat_combine(const int32_t *__restrict__ multi_chunk_begin,
-                              const int32_t *__restrict__ chunk_slot,
-                              const int32_t *__restrict__ chunk_begin,
-                              const int32_t *__restrict__ win, int64_t n_multi, int64_t H,
-                              int64_t F, int64_t n_nodes, const float *__restrict__ partial,
-                              float *__restrict__ out, int64_t ldo, float *row_max,
-                              float *row_sum) {
-    const int lane = threadIdx.x & 31;
-    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Merge the partials of windows spread over several chunks: one block per
+// (window, head), one warp per window row; the window's chunks are
+// [multi[2i], multi[2i+1]).  Row max and sum are reduced across the chunks
+// lane-parallel, then each lane merges its features over the chunks.
+__global__ void __launch_bounds__(kW * 32) k_gat_combine(
+    const int32_t *__restrict__ multi_chunk_begin, const int32_t *__restrict__ chunk_slot,
+    const int32_t *__restrict__ chunk_begin, const int32_t *__restrict__ win, int64_t n_multi,
+    int64_t H, int64_t F, int64_t n_nodes, const float *__restrict__ partial,
+    float *__restrict__ out, int64_t ldo, float *row_max, float *row_sum) {
+    const int lane = threadIdx.x & 31, r = threadIdx.x >> 5;
+    const int64_t wid = blockIdx.x;
     if (wid >= n_multi * H) return;
     const int64_t mwin = wid / H, h = wid - mwin * H;
     const int cb = multi_chunk_begin[2 * mwin], ce = multi_chunk_begin[2 * mwin + 1];
-    const int64_t wrow = (int64_t)win[chunk_begin[cb]] * kW;
-    for (int r = 0; r < kW; ++r) {
-        const int64_t row = wrow + r;
-        if (row >= n_nodes) break;
-        float m = -INFINITY;
+    const int64_t row = (int64_t)win[chunk_begin[cb]] * kW + r;
+    if (row >= n_nodes) return;
+    const int64_t pitch = kW * (F + 2);
+    auto part_row = [&](int c) {
+        return partial + ((int64_t)chunk_slot[c] * H + h) * pitch + r * (F + 2);
+    };
+    float m = -INFINITY;
+    for (int c = cb + lane; c < ce; c += 32) m = fmaxf(m, part_row(c)[F]);
+    m = warp_max(m);
+    const float mref = m == -INFINITY ? 0.f : m;
+    float l = 0.f;
+    for (int c = cb + lane; c < ce; c += 32) {
+        const float *pp = part_row(c);
+        l += __expf(pp[F] - mref) * pp[F + 1];
+    }
+    l = warp_sum(l);
+    const float inv = l > 0.f ? 1.f / l : 0.f;
+    for (int64_t f = lane; f < F; f += 32) {
+        float a = 0.f;
         for (int c = cb; c < ce; ++c) {
-            const float *pp = partial + ((int64_t)chunk_slot[c] * H + h) * kW * (F + 2) + r * (F + 2);
-            m = fmaxf(m, pp[F]);
+            const float *pp = part_row(c);
+            a += __expf(pp[F] - mref) * pp[f];
         }
-        const float mref = m == -INFINITY ? 0.f : m;
-        float l = 0.f;
-        for (int c = cb; c < ce; ++c) {
-            const float *pp = partial + ((int64_t)chunk_slot[c] * H + h) * kW * (F + 2) + r * (F + 2);
-            l += __expf(pp[F] - mref) * pp[F + 1];
-        }
-        const float inv = l > 0.f ? 1.f / l : 0.f;
-        for (int64_t f = lane; f < F; f += 32) {
-            float a = 0.f;
-            for (int c = cb; c < ce; ++c) {
-                const float *pp =
-                    partial + ((int64_t)chunk_slot[c] * H + h) * kW * (F + 2) + r * (F + 2);
-                a += __expf(pp[F] - mref) * pp[f];
-            }
-            out[row * ldo + h * F + f] = a * inv;
-        }
-        if (lane == 0) {
-            if (row_max) row_max[h * n_nodes + row] = m;
-            if (row_sum) row_sum[h * n_nodes + row] = l;
-        }
+        out[row * ldo + h * F + f] = a * inv;
+    }
+    if (lane == 0) {
+        if (row_max) row_max[h * n_nodes + row] = m;
+        if (row_sum) row_sum[h * n_nodes + row] = l;
     }
 }
 
@@ -595,27 +594,30 @@ struct BCfg {
     static constexpr int MT = F / 16;
 };
 
-template <typename T, int F, bool SPLIT>
+// IT: index type of items and element offsets (int32_t when every offset fits)
+template <typename T, int F, bool SPLIT, typename IT>
 __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
     using C = BCfg<T, F, SPLIT>;
+    const IT H = (IT)A.H, n_nodes = (IT)A.n_nodes, ldd = (IT)A.ldd, ldx = (IT)A.ldx,
+             ldg = (IT)A.ldg;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
     const unsigned char *sgen = smem + warp * C::WARP_SMEM;
     const int gid = lane >> 2, tig = lane & 3;
-    const int64_t n_items = A.n_parts * A.H;
-    const int64_t stride = (int64_t)gridDim.x * kGWarps;
+    const IT n_items = (IT)(A.n_parts * A.H);
+    const IT stride = (IT)gridDim.x * kGWarps;
     const T *Xq = (const T *)A.Xp;
     const T *D = (const T *)A.dout;
     const T *DL = (const T *)A.dout_lo;
 
-    int64_t p_item = (int64_t)blockIdx.x * kGWarps + warp;
-    int64_t p_h = 0;
+    IT p_item = (IT)blockIdx.x * kGWarps + warp;
+    IT p_h = 0;
     int p_start = 0, p_nreal = 0, p_pend = 0, p_step = 0, p_myc = -1;
     auto p_load = [&]() {
         while (p_item < n_items) {
-            const int64_t part = p_item / A.H;
-            p_h = p_item - part * A.H;
+            const IT part = p_item / H;
+            p_h = p_item - part * H;
             p_start = A.rowptr[2 * part];
             const int e = A.rowptr[2 * part + 1];
             p_pend = A.rowptr[2 * part + 2];
@@ -635,7 +637,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         const uint32_t cs = ms + C::MSTAGE;
         const int c0 = p_step * 16;
         int myc = p_myc;  // fetched one step ahead
-        if (myc >= A.n_nodes || myc < -1) {
+        if (myc >= n_nodes || myc < -1) {
             if (A.err) atomicOr(A.err, 1);
             myc = -1;
         }
@@ -646,7 +648,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
             const int cidx = __shfl_sync(0xffffffffu, myc, r & 15);
             if (idx < 16 * C::CPR) {
                 const bool ok = cidx >= 0;
-                const int64_t o = (int64_t)cidx * A.ldd + p_h * F + ch * 8;
+                const IT o = (IT)cidx * ldd + p_h * F + ch * 8;
                 const uint32_t d = r * C::XROW + ((ch ^ swz_row<F>(r)) << 4);
                 cp_async16(xs + d, ok ? D + o : D, ok ? 16 : 0);
                 if constexpr (SPLIT) cp_async16(xs + C::TILE + d, ok ? DL + o : DL, ok ? 16 : 0);
@@ -654,13 +656,13 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         }
         if (lane < 2) {
             const bool ok = c0 + 8 * lane < p_pend - p_start;
-            const int64_t bit0 = (int64_t)(p_start + c0 + 8 * lane) * kW;
+            const int64_t bit0 = (int64_t)(p_start + c0 + 8 * lane) * kW;  // bit index: 64-bit always
             cp_async8(ms + 8 * lane, ok ? (const void *)(A.mask + (bit0 >> 5)) : (const void *)A.mask,
                       ok ? 8 : 0);
         }
         if (lane < 16) {
             const bool ok = myc >= 0;
-            const int64_t o = p_h * A.n_nodes + (ok ? myc : 0);
+            const IT o = p_h * n_nodes + (ok ? myc : 0);
             const float *arrs[4] = {A.s0, A.m, A.l, A.c};
 #pragma unroll
             for (int a = 0; a < 4; ++a)
@@ -702,9 +704,9 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         mbit[u] = (c & ~wmask) * kW + r * A.wide + (c & wmask);
     }
     int cstage = 0, pstage = kGStages - 1;
-    for (int64_t c_item = (int64_t)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
-        const int64_t part = c_item / A.H;
-        const int64_t h = c_item - part * A.H;
+    for (IT c_item = (IT)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
+        const IT part = c_item / H;
+        const IT h = c_item - part * H;
         const int start = A.rowptr[2 * part];
         const int e = A.rowptr[2 * part + 1];
         const int pend = A.rowptr[2 * part + 2];
@@ -712,21 +714,21 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         if ((start & wmask) != 0 || (pend & wmask) != 0 || pend < start + nreal) nreal = 0;
         const int nsteps = (nreal + 15) >> 4;
         if (nsteps == 0) continue;
-        const int64_t wrow = (int64_t)A.win[part] * kW;
+        const IT wrow = (IT)A.win[part] * kW;
         uint32_t bq[C::MT][2];
 #pragma unroll
         for (int kk = 0; kk < C::MT; ++kk)
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
-                const int64_t row = wrow + gid;
+                const IT row = wrow + gid;
                 const int f = 16 * kk + 2 * tig + 8 * u;
-                bq[kk][u] = row < A.n_nodes ? *(const uint32_t *)(Xq + row * A.ldx + h * F + f) : 0u;
+                bq[kk][u] = row < n_nodes ? *(const uint32_t *)(Xq + row * ldx + h * F + f) : 0u;
             }
         float s1r[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-            const int64_t row = wrow + 2 * tig + u;
-            s1r[u] = row < A.n_nodes ? A.s1[h * A.n_nodes + row] : 0.f;
+            const IT row = wrow + 2 * tig + u;
+            s1r[u] = row < n_nodes ? A.s1[h * n_nodes + row] : 0.f;
         }
         float ds1_acc[2] = {0.f, 0.f};
         float acc[C::MT][4];
@@ -788,8 +790,8 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
                     const int ci = ((const int *)(cv + 64))[gid + 8 * u];  // -1 past nreal
-                    if (ci >= 0 && ci < A.n_nodes)
-                        red_add_f32(A.ds0 + h * A.n_nodes + ci, u ? c_hi : c_lo);
+                    if (ci >= 0 && ci < n_nodes)
+                        red_add_f32(A.ds0 + h * n_nodes + ci, u ? c_hi : c_lo);
                 }
             }
             // dX'_r += sum_c p[c][r] dout_c
@@ -822,15 +824,15 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         for (int j = 0; j < C::MT; ++j)
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const int64_t row = wrow + 2 * tig + (u & 1);
+                const IT row = wrow + 2 * tig + (u & 1);
                 const int f = 16 * j + gid + 8 * (u >> 1);
-                if (row < A.n_nodes) red_add_f32(A.dXp + row * A.ldg + h * F + f, acc[j][u]);
+                if (row < n_nodes) red_add_f32(A.dXp + row * ldg + h * F + f, acc[j][u]);
             }
         if (gid == 0) {
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
-                const int64_t row = wrow + 2 * tig + u;
-                if (row < A.n_nodes) red_add_f32(A.ds1 + h * A.n_nodes + row, ds1_acc[u]);
+                const IT row = wrow + 2 * tig + u;
+                if (row < n_nodes) red_add_f32(A.ds1 + h * n_nodes + row, ds1_acc[u]);
             }
         }
     }
@@ -840,24 +842,33 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
 template <typename T, int F, bool SPLIT>
 int run_gat_bwd(const GatBwdArgs &P, cudaStream_t st) {
     using C = BCfg<T, F, SPLIT>;
-    auto kernel = k_gat_backward<T, F, SPLIT>;
-    static std::once_flag once;
-    static int prep = ATT_OK;
-    std::call_once(once, [&] {
-        prep = cuda_status(
-            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
-            "cudaFuncSetAttribute");
-    });
-    if (prep != ATT_OK) return prep;
     const int64_t items = P.n_parts * P.H;
     if (items == 0) return ATT_OK;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGThreads, C::SMEM);
-    if (per_sm < 1) per_sm = 1;
-    const int64_t want = (items + kGWarps - 1) / kGWarps;
-    const int64_t cap = (int64_t)sm_count() * per_sm;
-    kernel<<<(unsigned)(want < cap ? want : cap), kGThreads, C::SMEM, st>>>(P);
-    return launch_status("k_gat_backward");
+    auto run = [&](auto kernel) {
+        static std::once_flag once;
+        static int prep = ATT_OK;
+        std::call_once(once, [&] {
+            prep = cuda_status(
+                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
+                "cudaFuncSetAttribute");
+        });
+        if (prep != ATT_OK) return prep;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGThreads, C::SMEM);
+        if (per_sm < 1) per_sm = 1;
+        const int64_t want = (items + kGWarps - 1) / kGWarps;
+        const int64_t cap = (int64_t)sm_count() * per_sm;
+        kernel<<<(unsigned)(want < cap ? want : cap), kGThreads, C::SMEM, st>>>(P);
+        return launch_status("k_gat_backward");
+    };
+    // 32-bit offsets when rows of X', dout and dXp, the per-head node arrays
+    // and the item count (plus one grid stride) all stay below 2^31
+    const int64_t lim = INT32_MAX - (1 << 22);
+    int64_t ld = P.ldx > P.ldd ? P.ldx : P.ldd;
+    ld = ld > P.ldg ? ld : P.ldg;
+    const bool small = P.n_nodes * ld < lim && P.n_nodes * P.H < lim && items < lim;
+    if (small) return run(k_gat_backward<T, F, SPLIT, int32_t>);
+    return run(k_gat_backward<T, F, SPLIT, int64_t>);
 }
 
 template <typename T>
@@ -939,8 +950,7 @@ extern "C" int att_gat_forward(const int32_t *rowptr, const int32_t *col, const 
                       : dispatch_gat_f<__nv_bfloat16, 1>(P, st, np);
     if (s != ATT_OK) return s;
     if (n_multi > 0) {
-        const int64_t threads = n_multi * n_heads * 32;
-        k_gat_combine<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+        k_gat_combine<<<(unsigned)(n_multi * n_heads), kW * 32, 0, st>>>(
             multi_chunk_begin, chunk_slot, chunk_begin, window_of_part, n_multi, n_heads, F,
             n_nodes, partial, out, ldo, row_max, row_sum);
         s = launch_status("k_gat_combine");
