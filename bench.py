@@ -588,8 +588,8 @@ DEFAULT_WORKLOAD = SpmmProducts.name
 
 # ---------------------------------------------------------------------------
 def _env_rank():
-    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
-            int(os.environ.get("WORLD_SIZE", 1)))
+    from att_gb300 import replicas
+    return replicas.env_rank()
 
 
 def cpu_baseline(wl, budget_s=12.0):
@@ -1006,13 +1006,12 @@ def main():
     total_ms = t_all0.elapsed_time(t_all1)
     per_launch = sorted(a.elapsed_time(b) for a, b in ev)
     avg_launch_ms = sum(per_launch) / len(per_launch)
-    t_max = torch.tensor([total_ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    total_ms = float(t_max.item())
+    from att_gb300 import replicas
+    total_ms = replicas.max_over_ranks([total_ms], device="cuda")[0]
     ms_per_step = total_ms / args.steps
     is_time = wl.unit == "ms"
-    value = ms_per_step if is_time else world * wl.bytes_alg / (ms_per_step * 1e-3) / 1e9
+    value = (ms_per_step if is_time
+             else replicas.aggregate_rate(wl.bytes_alg, ms_per_step, world) / 1e9)
     plain_ms = None
     if hasattr(wl, "plain_step"):
         for _ in range(2):
@@ -1045,10 +1044,7 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e_steps
-    e2e_ms_t = torch.tensor([e2e_ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(e2e_ms_t, op=dist.ReduceOp.MAX)
-    e2e_ms = float(e2e_ms_t.item())
+    e2e_ms = replicas.max_over_ranks([e2e_ms], device="cuda")[0]
 
     peak, peak_kind = peaks()
     kbytes = getattr(wl, "bytes_fused", wl.bytes_alg)
