@@ -254,6 +254,14 @@ class SpmmProducts(PipelinedE2E):
         ops.spmm(f.rowptr, f.col, self.val, f.window_of_part, f.atomic, self.Xk, self.n,
                  out=self.Y, x_scale=self.x_scale)
 
+    def autotune(self):
+        """Launch shape of att_spmm picked by the autotuner on this graph."""
+        from att_gb300 import autotune
+        choice, table = autotune.tune_spmm(self.fmt, self.Xk, self.n, x_scale=self.x_scale,
+                                           out=self.Y, val=self.val)
+        return {"choice": list(choice) if choice else None,
+                "ms_by_shape": {"/".join(str(v) for v in k): ms for k, ms in table.items()}}
+
     # end to end through the reference-facing drop-in, host buffers
     def e2e_setup(self):
         Xh = self.Xk.cpu().pin_memory()
@@ -714,7 +722,24 @@ def _serve_pool_and_model(scale):
     return pool, serving.GCN2(seed=SERVE_SEED)
 
 
-def _batched_roofline(pool, model, steps):
+def _tune_serving_groups(pool, model):
+    """Parts per work group of the batched SpMM, picked by the autotuner on
+    the pool's graphs (formats resident, layer-1 features)."""
+    import torch
+    from att_gb300 import autotune, serving
+    s = torch.cuda.current_stream()
+    reqs = [serving.Request(i, 0.0, rp, col, X, n, nnz) for i, (rp, col, X, n, nnz) in enumerate(pool)]
+    for r in reqs:
+        serving.prepare(r, model, s, with_groups=False)
+    torch.cuda.synchronize()
+    G, table = autotune.tune_group_parts(reqs)
+    for r in reqs:
+        r.dev = {}
+    torch.cuda.synchronize()
+    return G, table
+
+
+def _batched_roofline(pool, model, steps, group_parts):
     """Kernel-only timing of one batched launch over every pool graph (their
     formats resident), against the same graphs as one att_spmm call each."""
     import torch
@@ -722,7 +747,7 @@ def _batched_roofline(pool, model, steps):
     s = torch.cuda.current_stream()
     reqs = [serving.Request(i, 0.0, rp, col, X, n, nnz) for i, (rp, col, X, n, nnz) in enumerate(pool)]
     for r in reqs:
-        serving.prepare(r, model, s)
+        serving.prepare(r, model, s, group_parts=group_parts)
     torch.cuda.synchronize()
     jobs = [serving.Job(r.dev["fmt"], r.dev["groups"], r.dev["partial"], r.dev["X"], r.dev["Y"], r.n)
             for r in reqs]
@@ -810,8 +835,10 @@ def run_serving(args):
     t_setup = time.time()
     pool, model = _serve_pool_and_model(args.scale)
     count = max(args.steps, 20)
+    group_parts, group_ms = _tune_serving_groups(pool, model)
     reqs = serving.make_requests(pool, SERVE_RATE, count, SERVE_SEED)
-    srv = serving.Server(model, budget=120e9, max_active=64, workers=8, keep_outputs=False)
+    srv = serving.Server(model, budget=120e9, max_active=64, workers=8, keep_outputs=False,
+                         group_parts=group_parts)
     # warm-up to the steady state of a running server: a real-time trace of
     # another seed through both paths (the caching device and pinned-host
     # allocators then hold blocks for the concurrency the rate brings)
@@ -850,12 +877,13 @@ def run_serving(args):
     # split windows with atomics, so they differ by fp32 rounding only)
     vr = [serving.Request(r.rid, 0.0, r.rowptr, r.col, r.X, r.n, r.nnz) for r in reqs[:48]]
     vp = [serving.Request(r.rid, 0.0, r.rowptr, r.col, r.X, r.n, r.nnz) for r in reqs[:48]]
-    serving.Server(model, budget=120e9, max_active=64, workers=8).run(vr, realtime=False)
+    serving.Server(model, budget=120e9, max_active=64, workers=8,
+                   group_parts=group_parts).run(vr, realtime=False)
     serving.serve_one_by_one(vp, model, realtime=False)
     agree = max(float((a.out - b.out).abs().max() / b.out.abs().max().clamp_min(1e-30))
                 for a, b in zip(vr, vp))
     del vr, vp
-    roof_raw = _batched_roofline(pool, model, max(5, min(args.steps, 20)))
+    roof_raw = _batched_roofline(pool, model, max(5, min(args.steps, 20)), group_parts)
     peak, peak_kind = peaks()
     achieved = roof_raw["bytes"] / (roof_raw["batched_ms"] * 1e-3) / 1e9
     base = None if args.no_cpu_baseline else _cpu_serve_baseline(pool, model)
@@ -882,6 +910,8 @@ def run_serving(args):
                                          "mean_ms": pst["mean_ms"],
                                          "graphs_per_s": pst["graphs_per_s"]},
             "saturation_graphs_per_s": cap,
+            "autotune": {"group_parts": group_parts,
+                         "batched_launch_ms_by_group_parts": {str(k): v for k, v in group_ms.items()}},
             "max_rel_diff_vs_plain_48_requests": agree,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
@@ -969,6 +999,7 @@ def main():
     _lib.load()
 
     wl = WORKLOADS[args.workload]("cuda", scale=args.scale)
+    tuned = wl.autotune() if hasattr(wl, "autotune") else None
     check_err = wl.check()
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
@@ -1082,6 +1113,7 @@ def main():
                 "clocks": clocks,
                 "gflops": world * wl.flops / (ms_per_step * 1e-3) / 1e9,
                 "plain_dropin_ms_per_step": plain_ms,
+                "autotune": tuned,
                 "fp16_equivalent_gbs": (world * wl.bytes_fp16 / (ms_per_step * 1e-3) / 1e9
                                         if hasattr(wl, "bytes_fp16") else None),
                 "check_rel_err": check_err,

@@ -313,3 +313,37 @@ def test_host_output_equals_device_output(cuda):
     assert torch.equal(host, dev.Y.cpu())
     with pytest.raises(_lib.AttError):
         serving.host_device_pointer(torch.zeros(16))
+
+
+def test_autotune_group_parts(cuda):
+    """tune_group_parts times the batched launch for each group size on
+    prepared requests and returns the fastest; the batched result with that
+    size equals the default size's within fp32 summation order (1e-5)."""
+    from att_gb300 import autotune, serving
+    model = serving.GCN2(seed=4)
+    s = torch.cuda.current_stream()
+    reqs = []
+    for i, (kind, seed) in enumerate(KINDS):
+        rp, col = _graph(kind, seed)
+        n = rp.shape[0] - 1
+        gen = torch.Generator().manual_seed(seed)
+        X = (torch.rand(n, 128, generator=gen) * 2 - 1).half()
+        r = serving.Request(i, 0.0, rp.to(torch.int32), col.to(torch.int32), X, n, int(col.shape[0]))
+        serving.prepare(r, model, s, with_groups=False)
+        reqs.append(r)
+    torch.cuda.synchronize()
+    G, table = autotune.tune_group_parts(reqs, candidates=(1, 2, 4, 8),
+                                         tuner=autotune.Tuner(warmup=1, reps=3))
+    assert set(table) == {1, 2, 4, 8} and G == min(table, key=table.get)
+    outs = {}
+    for g_parts in (G, 4):
+        jobs = []
+        for r in reqs:
+            g = serving.spmm_groups(r.dev["fmt"], g_parts, m_out=r.n)
+            part = torch.empty(max(g.n_slots, 1) * 8 * 128, dtype=torch.float32, device="cuda")
+            jobs.append(serving.Job(r.dev["fmt"], g, part, r.dev["X"],
+                                    torch.empty(r.n, 128, device="cuda"), r.n))
+        serving.spmm_batched(jobs).check()
+        outs[g_parts] = [j.Y.cpu().numpy() for j in jobs]
+    for a, b in zip(outs[G], outs[4]):
+        assert oracle.rel_err(a, b) <= 1e-5

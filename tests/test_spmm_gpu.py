@@ -284,3 +284,55 @@ def test_fp8_register_dequant_flags_bad_column(cuda, fp8_mode):
                  x_scale=scale.cuda(), err_flag=err)
     torch.cuda.synchronize()
     assert int(err.item()) & 1 and bool(torch.isfinite(Y).all())
+
+
+@pytest.fixture
+def restore_spmm_options():
+    from att_gb300 import _lib
+    import ctypes
+    keys = (b"spmm_fc", b"spmm_stages", b"spmm_fp8", b"spmm_gather")
+    old = {}
+    for k in keys:
+        v = ctypes.c_int(0)
+        _lib.call("att_get_option", k, ctypes.byref(v))
+        old[k] = v.value
+    yield
+    for k, v in old.items():
+        _lib.call("att_set_option", k, v)
+
+
+@pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16, torch.float8_e4m3fn])
+def test_autotune_spmm_sets_a_measured_shape(cuda, restore_spmm_options, dtype):
+    """tune_spmm times every candidate shape, leaves the fastest set (read
+    back through att_get_option) and the tuned launch gives the default
+    shape's result (same arithmetic; atomics may reorder fp32 adds)."""
+    from att_gb300 import _lib, autotune, graphs, ops
+    import ctypes
+    rowptr, col = graphs.random_csr(2000, 2000, 25, seed=9, hub_rows=3, hub_len=1500)
+    deg = np.full(2000, 0.2, np.float16)
+    f = _format(rowptr, col, deg, 8, 8, 32)
+    X = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, (2000, 128)).astype(np.float32))
+    scale = None
+    val = f.val
+    if dtype == torch.float8_e4m3fn:
+        Xk, scale = _quant_e4m3(X)
+        Xk, scale = Xk.cuda(), scale.cuda()
+    else:
+        Xk = X.to(dtype).cuda()
+        val = f.val.to(dtype)
+    Y0 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale)
+    tuner = autotune.Tuner(warmup=1, reps=3)
+    choice, table = autotune.tune_spmm(f, Xk, 2000, x_scale=scale, val=val, tuner=tuner)
+    assert set(table) == set(autotune.spmm_candidates(dtype, 128))
+    assert choice == min(table, key=table.get)
+    got = {}
+    for k in (b"spmm_fc", b"spmm_stages", b"spmm_fp8"):
+        v = ctypes.c_int(0)
+        _lib.call("att_get_option", k, ctypes.byref(v))
+        got[k] = v.value
+    if choice[0] == "spmm":
+        assert (got[b"spmm_fc"], got[b"spmm_stages"]) == choice[1:]
+    else:
+        assert got[b"spmm_fp8"] == choice[1]
+    Y1 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale)
+    assert oracle.rel_err(Y1.cpu().numpy(), Y0.cpu().numpy()) <= 1e-6
