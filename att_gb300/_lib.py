@@ -58,6 +58,8 @@ _SIGNATURES = {
     "att_rowsum": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_vp, _c_int,
                             _c_i64, _c_i64, _c_i64, _c_vp, _c_i64, _c_i64, _c_i64, _c_vp]),
     "att_slot_mask": (_c_int, [_c_vp, _c_i64, _c_vp, _c_i64, _c_vp]),
+    "att_edge_softmax": (_c_int, [_c_vp, _c_i64, _c_vp, _c_i64, _c_i64, ctypes.c_float, _c_int,
+                                  _c_vp, _c_int, _c_i64, _c_vp, _c_vp, _c_vp]),
     "att_gat_grad_prepare": (_c_int, [_c_vp, _c_i64, _c_vp, _c_i64, _c_i64, _c_i64, _c_i64, _c_vp,
                                       _c_vp, _c_int, _c_i64, _c_vp, _c_vp]),
     "att_gat_grad_finish": (_c_int, [_c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_int,

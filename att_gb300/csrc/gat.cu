@@ -662,3 +662,74 @@ extern "C" int att_rowsum(const int32_t *rowptr, const int32_t *map,
                                                  n_heads, out, out_stride_h, out_stride_n, m_out);
     return launch_status("k_rowsum_slots");
 }
+
+// ---------------------------------------------------------------------------
+// Edge softmax over CSR rows (the unfused chain's softmax in one kernel)
+// ---------------------------------------------------------------------------
+namespace att {
+namespace {
+
+// One warp per (head, row): lanes stride the row's edges keeping an online
+// (max, sum) pair, merged across the warp; a second sweep writes
+// exp(e - max) / sum.  Optional LeakyReLU on the logits first.
+__global__ void k_edge_softmax(const int32_t *__restrict__ rowptr, int64_t n_rows,
+                               const float *__restrict__ logits, int64_t lsh, int64_t H,
+                               float slope, int leaky, void *out, int odt, int64_t osh,
+                               float *row_max, float *row_sum) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wid >= n_rows * H) return;
+    const int64_t h = wid / n_rows, r = wid - h * n_rows;
+    const int64_t b = rowptr[r], e = rowptr[r + 1];
+    const float *L = logits + h * lsh;
+    float m = -INFINITY, s = 0.f;
+    for (int64_t i = b + lane; i < e; i += 32) {
+        float x = L[i];
+        if (leaky) x = x > 0.f ? x : slope * x;
+        if (x > m) {
+            s = s * __expf(m - x) + 1.f;
+            m = x;
+        } else {
+            s += __expf(x - m);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float m2 = __shfl_xor_sync(0xffffffffu, m, o);
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+        const float mn = fmaxf(m, m2);
+        s = (m == -INFINITY ? 0.f : s * __expf(m - mn)) + (m2 == -INFINITY ? 0.f : s2 * __expf(m2 - mn));
+        m = mn;
+    }
+    const float inv = s > 0.f ? 1.f / s : 0.f;
+    for (int64_t i = b + lane; i < e; i += 32) {
+        float x = L[i];
+        if (leaky) x = x > 0.f ? x : slope * x;
+        st_any(out, odt, h * osh + i, __expf(x - m) * inv);
+    }
+    if (lane == 0) {
+        if (row_max) row_max[h * n_rows + r] = m;
+        if (row_sum) row_sum[h * n_rows + r] = s;
+    }
+}
+
+}  // namespace
+}  // namespace att
+
+extern "C" int att_edge_softmax(const int32_t *rowptr, int64_t n_rows, const float *logits,
+                                int64_t logit_stride_h, int64_t n_heads, float slope, int leaky,
+                                void *out, int out_dtype, int64_t out_stride_h, float *row_max,
+                                float *row_sum, void *stream) {
+    using namespace att;
+    clear_error();
+    ATT_CHECK(n_rows >= 0 && n_heads > 0, ATT_ERR_INVALID, "bad sizes");
+    ATT_CHECK(out_dtype == ATT_F32 || out_dtype == ATT_F16 || out_dtype == ATT_BF16,
+              ATT_ERR_UNSUPPORTED, "edge softmax writes fp32, fp16 or bf16");
+    if (n_rows == 0) return ATT_OK;
+    ATT_CHECK(rowptr && logits && out, ATT_ERR_INVALID, "null pointer");
+    const int64_t threads = n_rows * n_heads * 32;
+    k_edge_softmax<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        rowptr, n_rows, logits, logit_stride_h, n_heads, slope, leaky, out, out_dtype,
+        out_stride_h, row_max, row_sum);
+    return launch_status("k_edge_softmax");
+}

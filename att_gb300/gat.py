@@ -233,3 +233,44 @@ class GATConv(torch.nn.Module):
     def forward(self, X, graph):
         Xp = torch.mm(X.to(self.dtype), self.W.to(self.dtype))
         return GATAttention.apply(Xp, self.a0, self.a1, graph, self.heads, self.slope)
+
+
+class DotAttentionChain:
+    """One dot-product GAT aggregation as the reference composes it, a chain
+    of separate ops with per-edge intermediates
+    (end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198 with the SDDMM of
+    ATT_SDDMM_v1.sddmm_*_h_nnz): per-edge logits X'_i . X'_j on tensor cores
+    (att_sddmm), LeakyReLU, the row softmax (row max subtracted so exp cannot
+    overflow; torch segment reductions), then the SpMM of the normalised edge
+    values (att_gather_slot_values + att_spmm).  16-bit X' runs fp16/bf16
+    tensor-core ops; fp32 X' runs the TF32 kernels (3xTF32, fp32-accurate).
+    The fused kernel (GATGraph.attention, mode MODE_DOT) computes the same
+    layer without the nnz-sized intermediates."""
+
+    def __init__(self, rowptr, col, window=8, wide=8, part=32):
+        require_cuda()
+        from . import gat_ops
+        rowptr = torch.as_tensor(rowptr).to("cuda")
+        col = torch.as_tensor(col).to("cuda")
+        n = int(rowptr.shape[0]) - 1
+        if n % window:
+            pad = window - n % window
+            rowptr = torch.cat([rowptr, rowptr[-1:].expand(pad)])
+        fmt = ops.block_convert(rowptr.to(torch.int32), col.to(torch.int32), None, window=window,
+                                wide=wide, part=part, want_val=False, want_map=True, n_cols=n)
+        self.fmt, self.window, self.n_nodes, self.nnz = fmt, window, n, fmt.nnz
+        self.qmap = gat_ops.map_to_quad(fmt.map, window, wide)
+        self.csr_rowptr = rowptr[: n + 1].to(torch.int32).contiguous()
+
+    def __call__(self, Xp, slope=0.2):
+        from . import gat_ops
+        f, n = self.fmt, self.n_nodes
+        X3 = Xp.unsqueeze(0)
+        e = gat_ops.sddmm(f.rowptr, f.col, self.qmap, f.window_of_part, self.window, X3, X3,
+                          self.nnz, torch.float32)[0]
+        # LeakyReLU + row softmax (att_edge_softmax), values in X' dtype
+        p = torch.empty(self.nnz, dtype=Xp.dtype, device=Xp.device)
+        _lib.call("att_edge_softmax", _p(self.csr_rowptr), n, _p(e), self.nnz, 1, float(slope), 1,
+                  _p(p), _DT[Xp.dtype], self.nnz, None, None, _stream())
+        return gat_ops.spmm_edge(f.rowptr, f.col, self.qmap, f.window_of_part, f.atomic,
+                                 self.window, p, 0, 1, X3, n)[0]

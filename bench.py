@@ -415,13 +415,43 @@ class GatReddit(PipelinedE2E):
     def e2e_step(self):
         self._pipe_step(self._e2e_compute)
 
+    def plain_step(self):
+        """The reference's chain of separate ops for the same layer (SDDMM,
+        LeakyReLU, row softmax, SpMM of the edge values), same dtype."""
+        if getattr(self, "chain", None) is None:
+            from att_gb300 import gat
+            self.chain = gat.DotAttentionChain(self.rowptr, self.colidx)
+        return self.chain(self.torch.mm(self.X, self.W))
+
+    def sample_error(self, out, Xp, rows=2000):
+        """Error of the layer's output against the FP64 layer on the same X'
+        for the first `rows` rows (normwise max and Frobenius relative)."""
+        torch = self.torch
+        rows = min(rows, self.n)
+        rp = self.rowptr[: rows + 1].long()
+        col = self.colidx[: int(rp[-1])].long()
+        lengths = rp[1:] - rp[:-1]
+        ridx = torch.repeat_interleave(torch.arange(rows, device=rp.device), lengths)
+        Xd = Xp.double()
+        e = torch.nn.functional.leaky_relu((Xd[ridx] * Xd[col]).sum(1), 0.2)
+        m = torch.segment_reduce(e, "max", lengths=lengths, unsafe=True)
+        pe = torch.exp(e - m[ridx])
+        pe = pe / torch.segment_reduce(pe, "sum", lengths=lengths, unsafe=True)[ridx]
+        ref = torch.zeros(rows, Xp.shape[1], dtype=torch.float64, device=rp.device)
+        ref.index_add_(0, ridx, pe[:, None] * Xd[col])
+        d = out[:rows].double() - ref
+        return {"rows": rows, "max_rel": float(d.abs().max() / ref.abs().max()),
+                "fro_rel": float(d.norm() / ref.norm())}
+
     def check(self):
         """Size-independent property at full size: every output row is a convex
         combination of its neighbours' X' rows, so it lies within their
-        per-feature min/max (checked on a sample of rows against the CSR)."""
+        per-feature min/max (checked on a sample of rows against the CSR).
+        Also the error against the FP64 layer on a row sample."""
         torch = self.torch
         Xp = torch.mm(self.X, self.W).float()
         out, rmax, rsum = self.G.attention(Xp.half())
+        self.err_vs_fp64 = self.sample_error(out, Xp.half())
         rp = self.rowptr.long()
         worst = 0.0
         for r in torch.linspace(0, self.n - 1, 64).long().tolist():
@@ -573,6 +603,57 @@ class GatArxivTrain:
         raise NotImplementedError
 
 
+class GatRedditTF32(GatReddit):
+    """The same GAT layer in fp32: X' = X W in fp32, then the chain of
+    separate ops on the TF32 kernels (att_sddmm 3xTF32 logits, LeakyReLU,
+    row softmax, att_spmm 3xTF32 aggregation); the fused kernel takes 16-bit
+    X' only."""
+    name = "gat_reddit_tf32"
+    e2e_api = "att_gb300.gat.DotAttentionChain (C ABI att_sddmm + att_spmm, TF32) after torch.mm"
+    kernel_name = "DotAttentionChain (att_sddmm tf32 + softmax + att_gather_slot_values + att_spmm 3xTF32)"
+
+    def __init__(self, device, scale=1.0, light=False):
+        super().__init__(device, scale=scale, light=light)
+        self.X = self.X.float()
+        self.W = self.W.float()
+        F, n = self.F, self.n
+        self.config["workload"] = self.name
+        if light:
+            return
+        from att_gb300 import gat
+        self.chain = gat.DotAttentionChain(self.rowptr, self.colidx)
+        # the layer's algorithmic bytes with fp32 operands (as the fused count)
+        self.bytes_fused = 4 * (n + 1) + 4 * self.nnz + n * F * 4 + self.U * F * 4 + n * F * 4
+        self.bytes_alg = self.bytes_fused + 2 * n * F * 4
+        self.launches_per_step = 5
+        self.config.update({"x_dtype": "fp32 (TF32 tensor cores, 3xTF32 split)",
+                            "path": "chain of separate ops (per-edge logits and values)"})
+
+    def step(self):
+        self.chain(self.torch.mm(self.X, self.W))
+
+    plain_step = None
+
+    def prepare_kernel(self):
+        self.Xp = self.torch.mm(self.X, self.W)
+
+    def kernel_step(self):
+        self.chain(self.Xp)
+
+    def _e2e_compute(self, X, W):
+        return self.chain(self.torch.mm(X, W))
+
+    def e2e_setup(self):
+        super().e2e_setup()
+        self.h2d = self.n * self.F * 4 + self.F * self.F * 4
+
+    def check(self):
+        Xp = self.torch.mm(self.X, self.W)
+        out = self.chain(Xp)
+        self.err_vs_fp64 = self.sample_error(out, Xp)
+        return self.err_vs_fp64["max_rel"]
+
+
 class SpmmProductsBF16(SpmmProducts):
     """The same SpMM with BF16 features and BF16 block values."""
     name = "spmm_products_bf16"
@@ -589,6 +670,7 @@ class SpmmProductsFP8(SpmmProducts):
 
 
 WORKLOADS = {SpmmProducts.name: SpmmProducts, GatReddit.name: GatReddit,
+             GatRedditTF32.name: GatRedditTF32,
              GatArxivTrain.name: GatArxivTrain, SpmmProductsBF16.name: SpmmProductsBF16,
              SpmmProductsFP8.name: SpmmProductsFP8}
 DEFAULT_WORKLOAD = SpmmProducts.name
@@ -1044,7 +1126,7 @@ def main():
     value = (ms_per_step if is_time
              else replicas.aggregate_rate(wl.bytes_alg, ms_per_step, world) / 1e9)
     plain_ms = None
-    if hasattr(wl, "plain_step"):
+    if getattr(wl, "plain_step", None):
         for _ in range(2):
             wl.plain_step()
         torch.cuda.synchronize()
@@ -1098,7 +1180,8 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": wl.unit, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
                 "higher_is_better": not is_time, "scaling": "weak", "vs_baseline": None,
-                "dtype": "bf16" if "bf16" in wl.name else ("e4m3" if "fp8" in wl.name else "f16"),
+                "dtype": ("bf16" if "bf16" in wl.name else "e4m3" if "fp8" in wl.name
+                          else "tf32" if "tf32" in wl.name else "f16"),
                 "data": "synthetic",
                 "config": dict(wl.config),
                 "workload_ms_per_step": ms_per_step,

@@ -317,6 +317,19 @@ ATT_API int att_gat_backward(const int32_t *rowptr_t, const int32_t *col_t,
                    const float *row_sum, const float *c, float slope, float *dXp, int64_t ldg,
                    float *ds0, float *ds1, int32_t *err_flag, void *stream);
 
+/* Row softmax of per-edge logits over CSR rows, optionally after LeakyReLU:
+ * out[h][e] = exp(x_e - m_r) / l_r with x = LeakyReLU(logits[h][e]) when
+ * leaky != 0, m_r the row max and l_r = sum exp(x - m_r) (fp32; written to
+ * row_max / row_sum [H][n_rows] when not NULL; -inf and 0 for rows without
+ * edges).  out: fp32, fp16 or bf16, [H] rows of out_stride_h.  Replaces the
+ * exp -> rowsum -> divide ops of the reference's GAT composition
+ * (end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198), with the row max
+ * subtracted so exp cannot overflow. */
+ATT_API int att_edge_softmax(const int32_t *rowptr, int64_t n_rows, const float *logits,
+                   int64_t logit_stride_h, int64_t n_heads, float slope, int leaky, void *out,
+                   int out_dtype, int64_t out_stride_h, float *row_max, float *row_sum,
+                   void *stream);
+
 /* The elementwise ends of the fused GAT backward, one pass over [N, H*F]
  * each (no counterpart in the reference, whose backward does them as separate
  * torch ops between its extension calls:

@@ -62,3 +62,25 @@ def test_fused_gat_empty_rows_and_tail(cuda):
     assert oracle.rel_err(out.cpu().numpy()[None], ref) <= 1e-2
     empty = (rp[1:] - rp[:-1]) == 0
     assert torch.all(out.cpu()[empty] == 0)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float16, 1e-2), (torch.bfloat16, 1e-2),
+                                       (torch.float32, 1e-4)])
+def test_dot_attention_chain_vs_fp64_and_fused(cuda, dtype, tol):
+    """The reference-style chain of separate ops (SDDMM, LeakyReLU, softmax,
+    SpMM of edge values) for one dot-attention layer: within 1e-2 (fp16 /
+    bf16) or 1e-4 (fp32 features on the 3xTF32 kernels) of FP64 on the same
+    X'; the 16-bit chain agrees with the fused kernel within 1e-2."""
+    from att_gb300 import gat
+    n = 1500
+    rp, col = _graph(n, 40, 1.9, seed=8, hub=True)
+    chain = gat.DotAttentionChain(rp, col)
+    g = torch.Generator().manual_seed(5)
+    Xp = ((torch.rand(n, 64, generator=g) * 2 - 1) * 0.6).to(dtype)
+    out = chain(Xp.cuda())
+    ref = oracle.gat_dot_layer_fp64(rp.numpy(), col.numpy(), Xp.double().numpy()[None], n)[0]
+    err = oracle.rel_err(out.cpu().numpy(), ref)
+    assert err <= tol, err
+    if dtype != torch.float32:
+        fused, _, _ = gat.GATGraph(rp, col).attention(Xp.cuda(), mode=gat.MODE_DOT)
+        assert oracle.rel_err(out.cpu().numpy(), fused.cpu().numpy()) <= 1e-2

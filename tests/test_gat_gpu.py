@@ -188,3 +188,43 @@ def test_gat_v1_chain_matches_fp64_layer(cuda):
     ref = oracle.gat_layer_fp64(rp_np[: n + 1], col_np, Xp.double().cpu().numpy()[None],
                                 a0.double().cpu().numpy()[None], a1.double().cpu().numpy()[None], n)
     assert oracle.rel_err(h.float().cpu().numpy(), ref) <= 1e-2
+
+
+@pytest.mark.parametrize("odt", [torch.float32, torch.float16, torch.bfloat16])
+@pytest.mark.parametrize("H", [1, 3])
+def test_edge_softmax_vs_fp64(cuda, odt, H):
+    """att_edge_softmax (LeakyReLU then row softmax over CSR rows) against the
+    FP64 oracle: probabilities within the output type's rounding (fp32 1e-6,
+    fp16 1e-3, bf16 8e-3 relative), row max / sum in fp32 within 1e-6, rows
+    without edges report max -inf and sum 0; covers a hub row (longer than a
+    warp's sweep many times over) and empty rows."""
+    from att_gb300 import _lib, graphs
+    from att_gb300.ops import _DT, _p, _stream
+    rp, col = graphs.random_csr(500, 500, 30, seed=4, empty_frac=0.3, hub_rows=1, hub_len=450)
+    n, nnz = 500, int(rp[-1])
+    g = torch.Generator().manual_seed(H)
+    logits = (torch.randn(H, nnz, generator=g) * 6).cuda()
+    out = torch.full((H, nnz), float("nan"), dtype=odt, device="cuda")
+    rmax = torch.empty(H, n, device="cuda")
+    rsum = torch.empty(H, n, device="cuda")
+    _lib.call("att_edge_softmax", _p(torch.from_numpy(rp).cuda()), n, _p(logits), nnz, H, 0.2, 1,
+              _p(out), _DT[odt], nnz, _p(rmax), _p(rsum), _stream())
+    torch.cuda.synchronize()
+    tol = {torch.float32: 1e-6, torch.float16: 1e-3, torch.bfloat16: 8e-3}[odt]
+    lens = np.diff(rp)
+    for h in range(H):
+        x = logits[h].double().cpu().numpy()
+        x = np.where(x > 0, x, 0.2 * x)
+        ref = oracle.edge_softmax_fp64(rp, x[None])[0]
+        got = out[h].double().cpu().numpy()
+        assert np.all(np.abs(got - ref) <= tol * np.abs(ref) + 1e-7)
+        rows = np.repeat(np.arange(n), lens)
+        m_ref = np.full(n, -np.inf)
+        np.maximum.at(m_ref, rows, x)
+        s_ref = np.zeros(n)
+        np.add.at(s_ref, rows, np.exp(x - m_ref[rows]))
+        has = lens > 0
+        rm, rs = rmax[h].cpu().numpy(), rsum[h].cpu().numpy()
+        assert np.allclose(rm[has], m_ref[has], rtol=1e-6, atol=0)
+        assert np.allclose(rs[has], s_ref[has], rtol=1e-5, atol=0)
+        assert np.all(np.isneginf(rm[~has])) and np.all(rs[~has] == 0)
