@@ -121,22 +121,24 @@ __global__ void k_slot_edges(SlotEdgeArgs A) {
 
 // ---- dense block values through the map ------------------------------------------
 // out is in the layout of block width out_wide, the map in that of map_wide
-__global__ void k_gather_slots(const int32_t *__restrict__ map, int64_t n_slots, int W,
-                               int map_wide, int out_wide, const void *vals, int vdt, int64_t vsh,
-                               int64_t vse, int64_t H, void *out, int odt, int64_t osh) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_slots * H) return;
-    const int64_t h = i / n_slots, s = i - h * n_slots;
-    int64_t ms = s;
-    if (map_wide != out_wide) {
-        const int64_t blk = s / ((int64_t)W * out_wide), inb = s % ((int64_t)W * out_wide);
-        const int r = (int)(inb / out_wide);
-        const int64_t g = blk * out_wide + inb % out_wide;
-        ms = slot_of(g, r, W, map_wide);
+// (W, map_wide and out_wide are powers of two, given as log2); heads on y
+__global__ void k_gather_slots(const int32_t *__restrict__ map, int64_t n_slots, int lw,
+                               int lmw, int low, const void *vals, int vdt, int64_t vsh,
+                               int64_t vse, void *out, int odt, int64_t osh) {
+    const int64_t h = blockIdx.y;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_slots; s += stride) {
+        int64_t ms = s;
+        if (lmw != low) {
+            const int64_t blk = s >> (lw + low), inb = s & ((1 << (lw + low)) - 1);
+            const int r = (int)(inb >> low);
+            const int64_t g = (blk << low) | (inb & ((1 << low) - 1));
+            ms = ((g >> lmw) << (lmw + lw)) | ((int64_t)r << lmw) | (g & ((1 << lmw) - 1));
+        }
+        const int32_t e = map[ms];
+        const float v = e >= 0 ? ld_any(vals, vdt, h * vsh + (int64_t)e * vse) : 0.f;
+        st_any(out, odt, h * osh + s, v);
     }
-    const int32_t e = map[ms];
-    const float v = e >= 0 ? ld_any(vals, vdt, h * vsh + (int64_t)e * vse) : 0.f;
-    st_any(out, odt, h * osh + s, v);
 }
 
 // ---- row sums through the map -----------------------------------------------------------
@@ -257,6 +259,16 @@ __global__ void __launch_bounds__(kSThreads) k_sddmm16(SddmmArgs P) {
     const T *A = (const T *)P.A;
     const T *B = (const T *)P.B;
 
+    // slot of (step column cl, window row r) relative to the step's first slot:
+    // fixed per lane, since every step starts on a multiple of wide (4, 8, 16)
+    int lsl[C::NT][4];
+#pragma unroll
+    for (int t = 0; t < C::NT; ++t)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int cl = gid + 8 * (u >> 1), r = t * 8 + 2 * tig + (u & 1);
+            lsl[t][u] = (cl - cl % P.wide) * W + r * P.wide + cl % P.wide;
+        }
     for (int64_t item = (int64_t)blockIdx.x * kSWarps + warp; item < n_items; item += stride) {
         const int64_t part = item / P.H, h = item - part * P.H;
         const int start = P.rowptr[2 * part];
@@ -343,9 +355,7 @@ __global__ void __launch_bounds__(kSThreads) k_sddmm16(SddmmArgs P) {
                     const int cl = gid + 8 * (u >> 1);
                     const int r = t * 8 + 2 * tig + (u & 1);
                     if (c0 + cl < nreal) {
-                        const int64_t g = start + c0 + cl;
-                        const int64_t sl = slot_of(g, r, W, P.wide) - (int64_t)(start + c0) * W;
-                        const int32_t e = ms[sl];
+                        const int32_t e = ms[lsl[t][u]];
                         if (e >= 0) st_any(P.out, P.odt, h * P.osh + (int64_t)e * P.ose, acc[t][u]);
                     }
                 }
@@ -364,19 +374,40 @@ __device__ __forceinline__ void split_tf32s(float x, uint32_t &hi, uint32_t &lo)
     lo = f32_to_tf32(x - __uint_as_float(hi));
 }
 
+// the fp32 kernel also keeps each warp's window rows (W x FC, rows padded by
+// 4 floats against bank conflicts) in shared memory, after the stage ring
+template <int W, int FC>
+struct STf32 {
+    static constexpr int QROW = FC + 4;
+    static constexpr int QTILE = W * QROW * 4;
+    static constexpr int SMEM = SCfg<float, W, FC>::SMEM + kSWarps * QTILE;
+};
+
 template <int W, int FC>
 __global__ void __launch_bounds__(kSThreads) k_sddmm_tf32(SddmmArgs P) {
     using C = SCfg<float, W, FC>;
+    using Q = STf32<W, FC>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
     const unsigned char *sgen = smem + warp * C::WARP_SMEM;
+    float *qs = (float *)(smem + C::SMEM + warp * Q::QTILE);
     const int gid = lane >> 2, tig = lane & 3;
     const int64_t n_items = P.n_parts * P.H;
     const int64_t stride = (int64_t)gridDim.x * kSWarps;
     const float *A = (const float *)P.A;
     const float *B = (const float *)P.B;
 
+    // slot of (step column cl, window row r) relative to the step's first slot:
+    // fixed per lane, since every step starts on a multiple of wide (4, 8, 16)
+    int lsl[C::NT][4];
+#pragma unroll
+    for (int t = 0; t < C::NT; ++t)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int cl = gid + 8 * (u >> 1), r = t * 8 + 2 * tig + (u & 1);
+            lsl[t][u] = (cl - cl % P.wide) * W + r * P.wide + cl % P.wide;
+        }
     for (int64_t item = (int64_t)blockIdx.x * kSWarps + warp; item < n_items; item += stride) {
         const int64_t part = item / P.H, h = item - part * P.H;
         const int start = P.rowptr[2 * part];
@@ -385,6 +416,14 @@ __global__ void __launch_bounds__(kSThreads) k_sddmm_tf32(SddmmArgs P) {
         const int nsteps = (nreal + 15) >> 4;
         if (nsteps == 0) continue;
         const int64_t wrow = (int64_t)P.win[part] * W;
+        // the window rows (the B side), staged once per item
+        __syncwarp();
+        for (int q = lane; q < W * FC; q += 32) {
+            const int rr = q / FC, f = q % FC;
+            const int64_t row = wrow + rr;
+            qs[rr * Q::QROW + f] = (row < P.n_a && f < P.F) ? A[h * P.ash + row * P.asn + f] : 0.f;
+        }
+        __syncwarp();
         auto issue = [&](int stage, int step) {
             const uint32_t xs = sbase + stage * C::STAGE;
             const uint32_t ms = xs + C::XSTAGE;
@@ -438,13 +477,9 @@ __global__ void __launch_bounds__(kSThreads) k_sddmm_tf32(SddmmArgs P) {
 #pragma unroll
                 for (int t = 0; t < C::NT; ++t) {
                     uint32_t bh[2], bl[2];
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const int64_t row = wrow + t * 8 + gid;
-                        const int64_t f = 8 * kk + tig + 4 * u;
-                        const float v = (row < P.n_a && f < P.F) ? A[h * P.ash + row * P.asn + f] : 0.f;
-                        split_tf32s(v, bh[u], bl[u]);
-                    }
+                    const float *qr = qs + (t * 8 + gid) * Q::QROW + 8 * kk + tig;
+                    split_tf32s(qr[0], bh[0], bl[0]);
+                    split_tf32s(qr[4], bh[1], bl[1]);
                     mma_1688_tf32(acc[t], al[0], al[1], al[2], al[3], bh[0], bh[1]);
                     mma_1688_tf32(acc[t], ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
                     mma_1688_tf32(acc[t], ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
@@ -458,9 +493,7 @@ __global__ void __launch_bounds__(kSThreads) k_sddmm_tf32(SddmmArgs P) {
                     const int cl = gid + 8 * (u >> 1);
                     const int r = t * 8 + 2 * tig + (u & 1);
                     if (c0 + cl < nreal) {
-                        const int64_t g = start + c0 + cl;
-                        const int64_t sl = slot_of(g, r, W, P.wide) - (int64_t)(start + c0) * W;
-                        const int32_t e = ms[sl];
+                        const int32_t e = ms[lsl[t][u]];
                         if (e >= 0) st_any(P.out, P.odt, h * P.osh + (int64_t)e * P.ose, acc[t][u]);
                     }
                 }
@@ -504,7 +537,7 @@ template <int W, int FC>
 int run_sddmm32(const SddmmArgs &P, cudaStream_t st) {
     static std::once_flag once;
     static int prep = ATT_OK;
-    return sddmm_launch(k_sddmm_tf32<W, FC>, SCfg<float, W, FC>::SMEM, P.n_parts * P.H, P, st,
+    return sddmm_launch(k_sddmm_tf32<W, FC>, STf32<W, FC>::SMEM, P.n_parts * P.H, P, st,
                         once, prep);
 }
 
@@ -622,12 +655,18 @@ extern "C" int att_gather_slot_values(const int32_t *map, int64_t n_slots, int w
     ATT_CHECK(window > 0 && map_wide > 0 && out_wide > 0, ATT_ERR_INVALID, "bad layout");
     ATT_CHECK(n_slots % ((int64_t)window * (map_wide > out_wide ? map_wide : out_wide)) == 0,
               ATT_ERR_INVALID, "slot count is not a whole number of blocks");
-    const int64_t n = n_slots * n_heads;
-    if (n == 0) return ATT_OK;
+    auto lg2 = [](int v) { int l = 0; while ((1 << l) < v) ++l; return (1 << l) == v ? l : -1; };
+    const int lw = lg2(window), lmw = lg2(map_wide), low = lg2(out_wide);
+    ATT_CHECK(lw >= 0 && lmw >= 0 && low >= 0, ATT_ERR_UNSUPPORTED,
+              "window and block widths must be powers of two");
+    ATT_CHECK(n_heads < 65536, ATT_ERR_UNSUPPORTED, "too many heads");
+    if (n_slots == 0 || n_heads == 0) return ATT_OK;
     ATT_CHECK(map && vals && out, ATT_ERR_INVALID, "null pointer");
-    k_gather_slots<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        map, n_slots, window, map_wide, out_wide, vals, v_dtype, v_stride_h, v_stride_e, n_heads,
-        out, out_dtype, out_stride_h);
+    const int64_t want = (n_slots + 255) / 256, cap = (int64_t)sm_count() * 16;
+    const dim3 grid((unsigned)(want < cap ? want : cap), (unsigned)n_heads);
+    k_gather_slots<<<grid, 256, 0, (cudaStream_t)stream>>>(map, n_slots, lw, lmw, low, vals,
+                                                          v_dtype, v_stride_h, v_stride_e, out,
+                                                          out_dtype, out_stride_h);
     return launch_status("k_gather_slots");
 }
 
