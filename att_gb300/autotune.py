@@ -3,8 +3,9 @@
 Two shapes are tuned by measurement, not by a model:
 
 * ``att_spmm`` (one graph per call): features per work item and cp.async ring
-  depth of the 16-bit kernel (``spmm_fc`` x ``spmm_stages``), or the FP8
-  dequantization kernel (``spmm_fp8``).  The best pair depends on how many
+  depth of the 16-bit kernel (``spmm_fc`` x ``spmm_stages``) or of the fp32
+  (3xTF32) kernel (``spmm_tf32``), or the FP8 dequantization kernel
+  (``spmm_fp8``).  The best pair depends on how many
   warps stay resident against how deep each warp's prefetch is, which moves
   with F, the dtype and the graph's part lengths.
 * ``att_spmm_batched`` (the serving loop): parts per work group.  Larger
@@ -82,6 +83,8 @@ def spmm_candidates(x_dtype, F):
         return [("spmm", fc, st) for fc in fcs for st in (2, 3, 4)]
     if x_dtype == torch.float8_e4m3fn:
         return [("fp8", 1), ("fp8", 0)]
+    if x_dtype == torch.float32:
+        return [("tf32", k) for k in (0, 1, 2, 3)] if F > 32 else []
     return []
 
 
@@ -91,13 +94,15 @@ def _apply_spmm(c):
         _set("spmm_stages", c[2])
     elif c[0] == "fp8":
         _set("spmm_fp8", c[1])
+    elif c[0] == "tf32":
+        _set("spmm_tf32", c[1])
 
 
 def tune_spmm(fmt, X, m_out, x_scale=None, out=None, val=None, tuner=None):
     """Time att_spmm's launch shapes on this format and features (block
     values `val`, default the format's own), set the fastest as the
     process-wide options, and return (choice, {choice: ms}).  Shapes with
-    nothing to tune (fp32 features) return (None, {})."""
+    nothing to tune (fp32 features with F <= 32) return (None, {})."""
     tuner = tuner or _default
     F = int(X.shape[1])
     cands = spmm_candidates(X.dtype, F)

@@ -681,13 +681,13 @@ __global__ void __launch_bounds__(kThreads) k_spmm16_tma(
 // ---------------------------------------------------------------------------
 // fp32 operand kernel: 3xTF32 m16n8k8
 // ---------------------------------------------------------------------------
-template <int W, int FC, int WIDE>
+template <int W, int FC, int WIDE, int S = kStages>
 struct CfgTF32 {
     static constexpr int XROW = FC * 4;
     static constexpr int XSTAGE = 16 * XROW;
     static constexpr int VSTAGE = 16 * W * 4;
     static constexpr int STAGE = XSTAGE + VSTAGE;
-    static constexpr int WARP_SMEM = kStages * STAGE;
+    static constexpr int WARP_SMEM = S * STAGE;
     static constexpr int SMEM = kWarps * WARP_SMEM;
     static constexpr int CPR = FC / 4;
     static constexpr int RPP = 32 / CPR;
@@ -701,14 +701,14 @@ __device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) 
     lo = f32_to_tf32(x - __uint_as_float(hi));
 }
 
-template <int W, int FC, int WIDE>
+template <int W, int FC, int WIDE, int S>
 __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col,
     const float *__restrict__ val, const int32_t *__restrict__ win,
     const int32_t *__restrict__ atomic, int64_t n_parts, const float *__restrict__ X, int64_t n_x,
     int64_t F, int64_t ldx, float *__restrict__ Y, int64_t m_out, int64_t ldy, int n_chunks,
     int32_t *__restrict__ err) {
-    using C = CfgTF32<W, FC, WIDE>;
+    using C = CfgTF32<W, FC, WIDE, S>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = smem_u32(smem) + warp * C::WARP_SMEM;
@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
     p_load();
     p_fetch();
 #pragma unroll
-    for (int s = 0; s < kStages - 1; ++s) {
+    for (int s = 0; s < S - 1; ++s) {
         if (p_item < n_items) {
             issue(s);
             p_advance();
@@ -791,13 +791,13 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
 #pragma unroll
         for (int t = 0; t < C::NT; ++t) acc[j][t][0] = acc[j][t][1] = acc[j][t][2] = acc[j][t][3] = 0.f;
 
-    int cstage = 0, pstage = kStages - 1;
+    int cstage = 0, pstage = S - 1;
     for (int64_t c_item = (int64_t)blockIdx.x * kWarps + warp; c_item < n_items; c_item += stride) {
         const int64_t part = c_item / n_chunks;
         const int fc = (int)(c_item - part * n_chunks);
         const PartInfo pi = part_info<WIDE>(rowptr, part, err);
         for (int step = 0; step < pi.nsteps; ++step) {
-            cp_async_wait<kStages - 2>();
+            cp_async_wait<S - 2>();
             __syncwarp();
             const float *xsg = (const float *)(sgen + cstage * C::STAGE);
             const float *vsg = (const float *)(sgen + cstage * C::STAGE + C::XSTAGE);
@@ -839,8 +839,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
                 p_advance();
             }
             cp_async_commit();
-            cstage = cstage + 1 == kStages ? 0 : cstage + 1;
-            pstage = pstage + 1 == kStages ? 0 : pstage + 1;
+            cstage = cstage + 1 == S ? 0 : cstage + 1;
+            pstage = pstage + 1 == S ? 0 : pstage + 1;
         }
         const int wrow = __ldg(win + part);
         const bool add = __ldg(atomic + part) != 0;
@@ -1867,12 +1867,12 @@ int launch16_bulk(const int32_t *rowptr, const int32_t *col, const void *val, co
     return run(k_spmm16_bulk<T, S, int64_t>);
 }
 
-template <int W, int FC, int WIDE>
+template <int W, int FC, int WIDE, int S = kStages>
 int launch_tf32(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
                 const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
                 int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err, cudaStream_t st) {
-    using C = CfgTF32<W, FC, WIDE>;
-    auto kernel = k_spmm_tf32<W, FC, WIDE>;
+    using C = CfgTF32<W, FC, WIDE, S>;
+    auto kernel = k_spmm_tf32<W, FC, WIDE, S>;
     static std::once_flag once;
     static int prep = ATT_OK;
     std::call_once(once, [&] { prep = prepare(kernel, C::SMEM); });
@@ -1949,6 +1949,8 @@ int g_spmm_fc = 64;
 // features per item when F > 64), 0 = through an fp16 shared tile
 // (k_spmm_fp8); att_set_option("spmm_fp8", ...).
 int g_spmm_fp8 = 1;
+// fp32-feature (3xTF32) kernel shape; att_set_option("spmm_tf32", 0..3)
+int g_spmm_tf32 = 0;
 
 template <int W, int FC, int WIDE>
 int launch_fp8(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
@@ -2046,11 +2048,18 @@ int dispatch_fc32(const int32_t *rowptr, const int32_t *col, const void *val, co
                   const int32_t *atomic, int64_t n_parts, const void *X, int64_t n_x, int64_t F,
                   int64_t ldx, float *Y, int64_t m_out, int64_t ldy, int32_t *err,
                   cudaStream_t st) {
-    if (F <= 32)
-        return launch_tf32<W, 32, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
-                                        m_out, ldy, err, st);
-    return launch_tf32<W, 64, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
-                                    m_out, ldy, err, st);
+#define ATT_LTF(FCv, Sv)                                                                        \
+    return launch_tf32<W, FCv, WIDE, Sv>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, \
+                                         Y, m_out, ldy, err, st)
+    // shapes (features per item x ring depth): 0 = 64 x 4, 1 = 32 x 3,
+    // 2 = 32 x 4, 3 = 64 x 2 (F <= 32 always takes 32-feature items)
+    if (F <= 32 || g_spmm_tf32 == 1 || g_spmm_tf32 == 2) {
+        if (g_spmm_tf32 == 1) ATT_LTF(32, 3);
+        ATT_LTF(32, 4);
+    }
+    if (g_spmm_tf32 == 3) ATT_LTF(64, 2);
+    ATT_LTF(64, 4);
+#undef ATT_LTF
 }
 
 }  // namespace
@@ -2181,6 +2190,11 @@ extern "C" int att_set_option(const char *key, int value) {
         g_spmm_fc = value;
         return ATT_OK;
     }
+    if (strcmp(key, "spmm_tf32") == 0) {
+        ATT_CHECK(value >= 0 && value <= 3, ATT_ERR_INVALID, "spmm_tf32 must be 0..3");
+        g_spmm_tf32 = value;
+        return ATT_OK;
+    }
     if (strcmp(key, "spmm_fp8") == 0) {
         ATT_CHECK(value == 0 || value == 1, ATT_ERR_INVALID, "spmm_fp8 must be 0 or 1");
         g_spmm_fp8 = value;
@@ -2199,6 +2213,10 @@ extern "C" int att_get_option(const char *key, int *value) {
     }
     if (strcmp(key, "spmm_stages") == 0) {
         *value = g_spmm_stages;
+        return ATT_OK;
+    }
+    if (strcmp(key, "spmm_tf32") == 0) {
+        *value = g_spmm_tf32;
         return ATT_OK;
     }
     if (strcmp(key, "spmm_fp8") == 0) {

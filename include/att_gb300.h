@@ -68,7 +68,9 @@ enum att_dtype {
  *   "spmm_stages": ring depth of the 16-bit cp.async kernel (2, 3, 4).
  *   "spmm_fc":     features per work item for F > 64 (64, the default, or 128).
  *   "spmm_fp8":    FP8 feature kernel: 1 = dequantized in registers (default),
- *                  0 = dequantized through an fp16 shared-memory tile. */
+ *                  0 = dequantized through an fp16 shared-memory tile.
+ *   "spmm_tf32":   fp32-feature (3xTF32) kernel, features per item x ring
+ *                  depth: 0 = 64 x 4 (default), 1 = 32 x 3, 2 = 32 x 4, 3 = 64 x 2. */
 ATT_API int att_set_option(const char *key, int value);
 ATT_API int att_get_option(const char *key, int *value);
 

@@ -53,4 +53,5 @@ def test_spmm_candidates():
     assert ("spmm", 64, 3) in c16 and ("spmm", 128, 2) in c16 and len(c16) == 6
     assert all(c[1] == 64 for c in autotune.spmm_candidates(torch.bfloat16, 64))
     assert autotune.spmm_candidates(torch.float8_e4m3fn, 128) == [("fp8", 1), ("fp8", 0)]
-    assert autotune.spmm_candidates(torch.float32, 128) == []
+    assert autotune.spmm_candidates(torch.float32, 128) == [("tf32", k) for k in range(4)]
+    assert autotune.spmm_candidates(torch.float32, 32) == []

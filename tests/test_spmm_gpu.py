@@ -290,7 +290,7 @@ def test_fp8_register_dequant_flags_bad_column(cuda, fp8_mode):
 def restore_spmm_options():
     from att_gb300 import _lib
     import ctypes
-    keys = (b"spmm_fc", b"spmm_stages", b"spmm_fp8", b"spmm_gather")
+    keys = (b"spmm_fc", b"spmm_stages", b"spmm_fp8", b"spmm_gather", b"spmm_tf32")
     old = {}
     for k in keys:
         v = ctypes.c_int(0)
@@ -301,7 +301,8 @@ def restore_spmm_options():
         _lib.call("att_set_option", k, v)
 
 
-@pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16, torch.float8_e4m3fn])
+@pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16, torch.float8_e4m3fn,
+                                   torch.float32])
 def test_autotune_spmm_sets_a_measured_shape(cuda, restore_spmm_options, dtype):
     """tune_spmm times every candidate shape, leaves the fastest set (read
     back through att_get_option) and the tuned launch gives the default
@@ -326,13 +327,38 @@ def test_autotune_spmm_sets_a_measured_shape(cuda, restore_spmm_options, dtype):
     assert set(table) == set(autotune.spmm_candidates(dtype, 128))
     assert choice == min(table, key=table.get)
     got = {}
-    for k in (b"spmm_fc", b"spmm_stages", b"spmm_fp8"):
+    for k in (b"spmm_fc", b"spmm_stages", b"spmm_fp8", b"spmm_tf32"):
         v = ctypes.c_int(0)
         _lib.call("att_get_option", k, ctypes.byref(v))
         got[k] = v.value
     if choice[0] == "spmm":
         assert (got[b"spmm_fc"], got[b"spmm_stages"]) == choice[1:]
+    elif choice[0] == "tf32":
+        assert got[b"spmm_tf32"] == choice[1]
     else:
         assert got[b"spmm_fp8"] == choice[1]
     Y1 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale)
     assert oracle.rel_err(Y1.cpu().numpy(), Y0.cpu().numpy()) <= 1e-6
+
+
+@pytest.mark.parametrize("F", [64, 72, 128, 36])
+def test_tf32_shapes_vs_fp64(cuda, restore_spmm_options, F):
+    """Every fp32-feature kernel shape (spmm_tf32 0..3: 64 x 4, 32 x 3,
+    32 x 4, 64 x 2 features per item x ring depth) within 1e-4 of FP64,
+    including partial feature chunks, split windows and rows past the last
+    window."""
+    from att_gb300 import _lib, graphs, ops
+    rowptr, col = graphs.random_csr(2003, 2003, 25, seed=F, hub_rows=4, hub_len=1700,
+                                    empty_frac=0.2)
+    deg = np.full(2003, 0.3, np.float16)
+    f = _format(rowptr, col, deg, 8, 4, 8)
+    val = f.val.float()
+    X = torch.from_numpy(np.random.default_rng(F).uniform(-1, 1, (2003, F)).astype(np.float32))
+    ev = oracle.gcn_values(rowptr, col, deg).astype(np.float64)
+    ref = _ref(rowptr, col, ev, X.double().numpy(), 2010, 8)
+    for shape in range(4):
+        _lib.call("att_set_option", b"spmm_tf32", shape)
+        Y = torch.full((2010, F), float("nan"), device="cuda")
+        ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, X.cuda(), 2010, window=8,
+                 wide=4, out=Y)
+        assert oracle.rel_err(Y.cpu().numpy(), ref) <= 1e-4, shape
