@@ -99,17 +99,32 @@ __device__ __forceinline__ int swz_row(int r) {
 
 template <typename T, int F, int MODE>
 struct GCfg {
-    static constexpr int XROW = F * 2;
+    static constexpr bool F32 = sizeof(T) == 4;  // fp32 X': 3xTF32 products
+    static constexpr int XROW = F * (int)sizeof(T);
     static constexpr int XSTAGE = 16 * XROW;
     static constexpr int MSTAGE = 16;            // 128 occupancy bits
     static constexpr int SSTAGE = MODE == 1 ? 64 : 0;  // s1 of the 16 columns
     static constexpr int STAGE = XSTAGE + MSTAGE + SSTAGE;
-    static constexpr int WARP_SMEM = kGStages * STAGE;
+    static constexpr int PTILE = F32 ? 16 * kW * 4 : 0;  // the step's P, re-read transposed
+    static constexpr int WARP_SMEM = kGStages * STAGE + PTILE;
     static constexpr int SMEM = kGWarps * WARP_SMEM;
     static constexpr int CPR = XROW / 16;
+    static constexpr int EPC = 16 / (int)sizeof(T);  // elements per 16-byte chunk
     static constexpr int PASSES = (16 * CPR + 31) / 32;
     static constexpr int MT = F / 16;
 };
+
+// XOR swizzle of 16-byte chunks by row, for rows of ROW_BYTES bytes
+template <int ROW_BYTES>
+__device__ __forceinline__ int swz_rb(int r) {
+    if constexpr (ROW_BYTES >= 128) return r & 7;
+    else return (r >> 1) & 3;
+}
+
+__device__ __forceinline__ void split_tf32f(float x, uint32_t &hi, uint32_t &lo) {
+    hi = f32_to_tf32(x);
+    lo = f32_to_tf32(x - __uint_as_float(hi));
+}
 
 // PSPLIT: aggregate with P as a hi + lo pair of 16-bit values (fp32-accurate
 // output); the training path needs it so that dout . out matches the
@@ -128,6 +143,8 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     const IT H = (IT)A.H, n_nodes = (IT)A.n_nodes, ldx = (IT)A.ldx, ldo = (IT)A.ldo;
     const T *X = (const T *)A.X;
     const float NEG_INF = -INFINITY;
+    float *ptile = (float *)(smem + warp * C::WARP_SMEM + kGStages * C::STAGE);  // fp32 only
+    (void)ptile;
 
     // ---- producer: (item, part, step) cursor ----
     IT p_item = (IT)blockIdx.x * kGWarps + warp;
@@ -183,8 +200,8 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
             const int cidx = __shfl_sync(0xffffffffu, myc, r & 15);
             if (idx < 16 * C::CPR) {
                 const bool ok = cidx >= 0;
-                const IT off = ok ? (IT)cidx * ldx + p_h * F + ch * 8 : (IT)0;
-                cp_async16(xs + r * C::XROW + ((ch ^ swz_row<F>(r)) << 4), X + off, ok ? 16 : 0);
+                const IT off = ok ? (IT)cidx * ldx + p_h * F + ch * C::EPC : (IT)0;
+                cp_async16(xs + r * C::XROW + ((ch ^ swz_rb<C::XROW>(r)) << 4), X + off, ok ? 16 : 0);
             }
         }
         // occupancy bits of the step's 16 x 8 slots, one 8-byte piece per
@@ -247,10 +264,12 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
         const int part0 = A.chunk_begin[chunk], part1 = A.chunk_begin[chunk + 1];
         if (part1 <= part0) continue;
         const IT wrow = (IT)A.win[part0] * kW;
-        // query side of the window: B fragments (mode 0) or row scores (mode 1)
+        // query side of the window: B fragments (mode 0) or row scores (mode 1);
+        // fp32: the B values of every 8-feature k-step, split at use
         uint32_t bq[C::MT][2];
+        float bqf[C::F32 ? F / 8 : 1][2];
         float s0r[2] = {0.f, 0.f};
-        if constexpr (MODE == 0) {
+        if constexpr (MODE == 0 && !C::F32) {
 #pragma unroll
             for (int kk = 0; kk < C::MT; ++kk)
 #pragma unroll
@@ -258,6 +277,15 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                     const IT row = wrow + gid;
                     const int f = 16 * kk + 2 * tig + 8 * u;
                     bq[kk][u] = row < n_nodes ? *(const uint32_t *)(X + (row * ldx + h * F + f)) : 0u;
+                }
+        } else if constexpr (MODE == 0) {
+#pragma unroll
+            for (int kk = 0; kk < F / 8; ++kk)
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const IT row = wrow + gid;
+                    const int f = 8 * kk + tig + 4 * u;
+                    bqf[kk][u] = row < n_nodes ? (float)X[row * ldx + h * F + f] : 0.f;
                 }
         } else {
 #pragma unroll
@@ -285,7 +313,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                 const uint32_t *mw = (const uint32_t *)(sgen + cstage * C::STAGE + C::XSTAGE);
                 // logits S[col][row]: this lane holds cols (gid, gid+8) x rows (2tig, 2tig+1)
                 float sv[4];
-                if constexpr (MODE == 0) {
+                if constexpr (MODE == 0 && !C::F32) {
                     sv[0] = sv[1] = sv[2] = sv[3] = 0.f;
 #pragma unroll
                     for (int kk = 0; kk < C::MT; ++kk) {
@@ -293,9 +321,30 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                         const int mrow = (q & 1) * 8 + rr;
                         const int ch = 2 * kk + (q >> 1);
                         uint32_t a[4];
-                        ldsm_x4(xs + mrow * C::XROW + ((ch ^ swz_row<F>(mrow)) << 4), a[0], a[1],
+                        ldsm_x4(xs + mrow * C::XROW + ((ch ^ swz_rb<C::XROW>(mrow)) << 4), a[0], a[1],
                                 a[2], a[3]);
                         mma_16816<T>(sv, a, bq[kk][0], bq[kk][1]);
+                    }
+                } else if constexpr (MODE == 0) {
+                    // 8 features per k-step; ldmatrix of 16-byte rows hands each
+                    // lane the fp32 element (row gid, feature tig) of every 8 x 4
+                    // matrix: the m16n8k8 A fragment.  3xTF32: lo.hi + hi.lo + hi.hi
+                    sv[0] = sv[1] = sv[2] = sv[3] = 0.f;
+#pragma unroll
+                    for (int kk = 0; kk < F / 8; ++kk) {
+                        const int q = lane >> 3, rr = lane & 7;
+                        const int mrow = (q & 1) * 8 + rr;
+                        const int ch = 2 * kk + (q >> 1);
+                        uint32_t a[4], ah[4], al[4], bh[2], bl[2];
+                        ldsm_x4(xs + mrow * C::XROW + ((ch ^ swz_rb<C::XROW>(mrow)) << 4), a[0], a[1],
+                                a[2], a[3]);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) split_tf32f(__uint_as_float(a[u]), ah[u], al[u]);
+                        split_tf32f(bqf[kk][0], bh[0], bl[0]);
+                        split_tf32f(bqf[kk][1], bh[1], bl[1]);
+                        mma_1688_tf32(sv, al[0], al[1], al[2], al[3], bh[0], bh[1]);
+                        mma_1688_tf32(sv, ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
+                        mma_1688_tf32(sv, ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
                     }
                 } else {
                     const float *s1s = (const float *)(sgen + cstage * C::STAGE + C::XSTAGE + C::MSTAGE);
@@ -351,26 +400,60 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                         acc[j][3] *= alpha[1];
                     }
                 }
-                // P^T into B fragments: (col gid, rows 2tig..) -> (row gid, cols 2tig..)
-                const uint32_t h01 = pack2<T>(p[0], p[1]), h23 = pack2<T>(p[2], p[3]);
-                const uint32_t b0 = movmatrix_trans(h01);
-                const uint32_t b1 = movmatrix_trans(h23);
-                uint32_t bl0 = 0, bl1 = 0;
-                if constexpr (PSPLIT) {
-                    const float2 r01 = unpack2<T>(h01), r23 = unpack2<T>(h23);
-                    bl0 = movmatrix_trans(pack2<T>(p[0] - r01.x, p[1] - r01.y));
-                    bl1 = movmatrix_trans(pack2<T>(p[2] - r23.x, p[3] - r23.y));
-                }
+                if constexpr (!C::F32) {
+                    // P^T into B fragments: (col gid, rows 2tig..) -> (row gid, cols 2tig..)
+                    const uint32_t h01 = pack2<T>(p[0], p[1]), h23 = pack2<T>(p[2], p[3]);
+                    const uint32_t b0 = movmatrix_trans(h01);
+                    const uint32_t b1 = movmatrix_trans(h23);
+                    uint32_t bl0 = 0, bl1 = 0;
+                    if constexpr (PSPLIT) {
+                        const float2 r01 = unpack2<T>(h01), r23 = unpack2<T>(h23);
+                        bl0 = movmatrix_trans(pack2<T>(p[0] - r01.x, p[1] - r01.y));
+                        bl1 = movmatrix_trans(pack2<T>(p[2] - r23.x, p[3] - r23.y));
+                    }
 #pragma unroll
-                for (int j = 0; j < C::MT; ++j) {
-                    const int q = lane >> 3, rr = lane & 7;
-                    const int k = (q >> 1) * 8 + rr;
-                    const int ch = 2 * j + (q & 1);
-                    uint32_t a[4];
-                    ldsm_x4_trans(xs + k * C::XROW + ((ch ^ swz_row<F>(k)) << 4), a[0], a[1], a[2],
-                                  a[3]);
-                    mma_16816<T>(acc[j], a, b0, b1);
-                    if constexpr (PSPLIT) mma_16816<T>(acc[j], a, bl0, bl1);
+                    for (int j = 0; j < C::MT; ++j) {
+                        const int q = lane >> 3, rr = lane & 7;
+                        const int k = (q >> 1) * 8 + rr;
+                        const int ch = 2 * j + (q & 1);
+                        uint32_t a[4];
+                        ldsm_x4_trans(xs + k * C::XROW + ((ch ^ swz_rb<C::XROW>(k)) << 4), a[0], a[1],
+                                      a[2], a[3]);
+                        mma_16816<T>(acc[j], a, b0, b1);
+                        if constexpr (PSPLIT) mma_16816<T>(acc[j], a, bl0, bl1);
+                    }
+                } else {
+                    // P through shared memory: written as (col, row), read back as the
+                    // m16n8k8 B fragment (col tig (+4), row gid) of each 8-column k-step
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        ptile[(gid + 8 * (u >> 1)) * kW + 2 * tig + (u & 1)] = p[u];
+                    __syncwarp();
+                    uint32_t ph[2][2], pl[2][2];
+#pragma unroll
+                    for (int ks = 0; ks < 2; ++ks) {
+                        split_tf32f(ptile[(8 * ks + tig) * kW + gid], ph[ks][0], pl[ks][0]);
+                        split_tf32f(ptile[(8 * ks + tig + 4) * kW + gid], ph[ks][1], pl[ks][1]);
+                    }
+                    const float *xt = (const float *)(sgen + cstage * C::STAGE);
+#pragma unroll
+                    for (int j = 0; j < C::MT; ++j) {
+#pragma unroll
+                        for (int ks = 0; ks < 2; ++ks) {
+                            // A = X'^T: (feature 16j + gid (+8), column 8ks + tig (+4))
+                            uint32_t ah[4], al[4];
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                const int c = 8 * ks + tig + 4 * (u >> 1);
+                                const int f = 16 * j + gid + 8 * (u & 1);
+                                const float x = xt[c * F + (((f >> 2) ^ swz_rb<C::XROW>(c)) << 2) + (f & 3)];
+                                split_tf32f(x, ah[u], al[u]);
+                            }
+                            mma_1688_tf32(acc[j], al[0], al[1], al[2], al[3], ph[ks][0], ph[ks][1]);
+                            mma_1688_tf32(acc[j], ah[0], ah[1], ah[2], ah[3], pl[ks][0], pl[ks][1]);
+                            mma_1688_tf32(acc[j], ah[0], ah[1], ah[2], ah[3], ph[ks][0], ph[ks][1]);
+                        }
+                    }
                 }
                 __syncwarp();
                 if (p_item < n_items) {
@@ -537,14 +620,27 @@ int run_gat(const GatArgs &P, cudaStream_t st, int64_t n_partial) {
 
 template <typename T, int MODE>
 int dispatch_gat_f(const GatArgs &P, cudaStream_t st, int64_t np) {
-    const bool split = P.row_sum != nullptr;  // statistics requested: training path
-    switch (P.F) {
-        case 32: return split ? run_gat<T, 32, MODE, true>(P, st, np) : run_gat<T, 32, MODE, false>(P, st, np);
-        case 64: return split ? run_gat<T, 64, MODE, true>(P, st, np) : run_gat<T, 64, MODE, false>(P, st, np);
-        case 128: return split ? run_gat<T, 128, MODE, true>(P, st, np) : run_gat<T, 128, MODE, false>(P, st, np);
-        default:
-            set_error("fused GAT supports F in {32, 64, 128}, got %lld", (long long)P.F);
-            return ATT_ERR_UNSUPPORTED;
+    // statistics requested: training path (16-bit P as hi + lo); fp32 X'
+    // always runs 3xTF32 products
+    const bool split = P.row_sum != nullptr && sizeof(T) == 2;
+    if constexpr (sizeof(T) == 4) {
+        switch (P.F) {
+            case 32: return run_gat<T, 32, MODE, false>(P, st, np);
+            case 64: return run_gat<T, 64, MODE, false>(P, st, np);
+            case 128: return run_gat<T, 128, MODE, false>(P, st, np);
+            default:
+                set_error("fused GAT supports F in {32, 64, 128}, got %lld", (long long)P.F);
+                return ATT_ERR_UNSUPPORTED;
+        }
+    } else {
+        switch (P.F) {
+            case 32: return split ? run_gat<T, 32, MODE, true>(P, st, np) : run_gat<T, 32, MODE, false>(P, st, np);
+            case 64: return split ? run_gat<T, 64, MODE, true>(P, st, np) : run_gat<T, 64, MODE, false>(P, st, np);
+            case 128: return split ? run_gat<T, 128, MODE, true>(P, st, np) : run_gat<T, 128, MODE, false>(P, st, np);
+            default:
+                set_error("fused GAT supports F in {32, 64, 128}, got %lld", (long long)P.F);
+                return ATT_ERR_UNSUPPORTED;
+        }
     }
 }
 
@@ -916,11 +1012,12 @@ extern "C" int att_gat_forward(const int32_t *rowptr, const int32_t *col, const 
     ATT_CHECK(window == kW, ATT_ERR_UNSUPPORTED, "fused GAT needs 8-row windows");
     ATT_CHECK(wide == 4 || wide == 8 || wide == 16, ATT_ERR_UNSUPPORTED, "wide must be 4, 8 or 16");
     ATT_CHECK(mode == 0 || mode == 1, ATT_ERR_INVALID, "mode must be 0 (dot) or 1 (additive)");
-    ATT_CHECK(x_dtype == ATT_F16 || x_dtype == ATT_BF16, ATT_ERR_UNSUPPORTED,
-              "fused GAT takes fp16 or bf16 features");
+    ATT_CHECK(x_dtype == ATT_F16 || x_dtype == ATT_BF16 || x_dtype == ATT_F32, ATT_ERR_UNSUPPORTED,
+              "fused GAT takes fp16, bf16 or fp32 (3xTF32) features");
     ATT_CHECK(n_heads > 0 && n_heads <= 32 && F > 0, ATT_ERR_INVALID, "bad heads / features");
-    ATT_CHECK(ldx % 8 == 0 && ((uintptr_t)Xp & 15) == 0 && ldx >= n_heads * F, ATT_ERR_UNSUPPORTED,
-              "X' rows must be 16-byte aligned with ldx >= heads*F");
+    ATT_CHECK(ldx % (x_dtype == ATT_F32 ? 4 : 8) == 0 && ((uintptr_t)Xp & 15) == 0 &&
+                  ldx >= n_heads * F,
+              ATT_ERR_UNSUPPORTED, "X' rows must be 16-byte aligned with ldx >= heads*F");
     ATT_CHECK(ldo >= n_heads * F, ATT_ERR_INVALID, "ldo < heads*F");
     ATT_CHECK(mode == 0 || (s0 && s1), ATT_ERR_INVALID, "additive mode needs node scores");
     cudaStream_t st = (cudaStream_t)stream;
@@ -945,6 +1042,8 @@ extern "C" int att_gat_forward(const int32_t *rowptr, const int32_t *col, const 
     const int64_t np = P.n_chunks;
     if (x_dtype == ATT_F16)
         s = mode == 0 ? dispatch_gat_f<__half, 0>(P, st, np) : dispatch_gat_f<__half, 1>(P, st, np);
+    else if (x_dtype == ATT_F32)
+        s = mode == 0 ? dispatch_gat_f<float, 0>(P, st, np) : dispatch_gat_f<float, 1>(P, st, np);
     else
         s = mode == 0 ? dispatch_gat_f<__nv_bfloat16, 0>(P, st, np)
                       : dispatch_gat_f<__nv_bfloat16, 1>(P, st, np);

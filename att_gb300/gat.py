@@ -130,8 +130,8 @@ class GATGraph:
 
     def attention(self, Xp, n_heads=1, mode=MODE_DOT, s0=None, s1=None, slope=0.2, out=None,
                   stats=True):
-        """Fused GAT aggregation.  Xp: [n_nodes, n_heads*F] fp16/bf16 (projected
-        features).  mode MODE_DOT: logits X'_i . X'_j per head; MODE_ADD: logits
+        """Fused GAT aggregation.  Xp: [n_nodes, n_heads*F] fp16/bf16, or fp32
+        for TF32 tensor cores with 3xTF32 products (projected features).  mode MODE_DOT: logits X'_i . X'_j per head; MODE_ADD: logits
         s0[h][i] + s1[h][j] (fp32 [n_heads, n_nodes]).  Returns
         (out fp32 [n_nodes, n_heads*F], row_max, row_sum) with the fp32 softmax
         statistics [n_heads, n_nodes] (None if not ``stats``)."""

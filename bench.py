@@ -604,13 +604,13 @@ class GatArxivTrain:
 
 
 class GatRedditTF32(GatReddit):
-    """The same GAT layer in fp32: X' = X W in fp32, then the chain of
-    separate ops on the TF32 kernels (att_sddmm 3xTF32 logits, LeakyReLU,
-    row softmax, att_spmm 3xTF32 aggregation); the fused kernel takes 16-bit
-    X' only."""
+    """The same GAT layer in fp32: X' = X W in fp32, then the fused kernel on
+    TF32 tensor cores (3xTF32 logits and aggregation); the plain comparison
+    is the chain of separate ops on the TF32 kernels (att_sddmm, row softmax,
+    att_spmm)."""
     name = "gat_reddit_tf32"
-    e2e_api = "att_gb300.gat.DotAttentionChain (C ABI att_sddmm + att_spmm, TF32) after torch.mm"
-    kernel_name = "DotAttentionChain (att_sddmm tf32 + softmax + att_gather_slot_values + att_spmm 3xTF32)"
+    e2e_api = "att_gb300.gat.GATGraph.attention (C ABI att_gat_forward, fp32 / 3xTF32) after torch.mm"
+    kernel_name = "att_gat_forward fp32 (k_gat_zero_rows + k_gat_fused<float> + k_gat_combine)"
 
     def __init__(self, device, scale=1.0, light=False):
         super().__init__(device, scale=scale, light=light)
@@ -625,23 +625,24 @@ class GatRedditTF32(GatReddit):
         # the layer's algorithmic bytes with fp32 operands (as the fused count)
         self.bytes_fused = 4 * (n + 1) + 4 * self.nnz + n * F * 4 + self.U * F * 4 + n * F * 4
         self.bytes_alg = self.bytes_fused + 2 * n * F * 4
-        self.launches_per_step = 5
         self.config.update({"x_dtype": "fp32 (TF32 tensor cores, 3xTF32 split)",
-                            "path": "chain of separate ops (per-edge logits and values)"})
+                            "path": "fused kernel; plain = chain of separate ops"})
 
     def step(self):
-        self.chain(self.torch.mm(self.X, self.W))
+        self.G.attention(self.torch.mm(self.X, self.W), out=self.out, stats=False)
 
-    plain_step = None
+    def plain_step(self):
+        return self.chain(self.torch.mm(self.X, self.W))
 
     def prepare_kernel(self):
         self.Xp = self.torch.mm(self.X, self.W)
 
     def kernel_step(self):
-        self.chain(self.Xp)
+        self.G.attention(self.Xp, out=self.out, stats=False)
 
     def _e2e_compute(self, X, W):
-        return self.chain(self.torch.mm(X, W))
+        out, _, _ = self.G.attention(self.torch.mm(X, W), stats=False)
+        return out
 
     def e2e_setup(self):
         super().e2e_setup()
@@ -649,8 +650,10 @@ class GatRedditTF32(GatReddit):
 
     def check(self):
         Xp = self.torch.mm(self.X, self.W)
-        out = self.chain(Xp)
+        out, _, _ = self.G.attention(Xp)
         self.err_vs_fp64 = self.sample_error(out, Xp)
+        chain = self.chain(Xp)
+        self.chain_err_vs_fp64 = self.sample_error(chain, Xp)
         return self.err_vs_fp64["max_rel"]
 
 

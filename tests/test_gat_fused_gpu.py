@@ -84,3 +84,34 @@ def test_dot_attention_chain_vs_fp64_and_fused(cuda, dtype, tol):
     if dtype != torch.float32:
         fused, _, _ = gat.GATGraph(rp, col).attention(Xp.cuda(), mode=gat.MODE_DOT)
         assert oracle.rel_err(out.cpu().numpy(), fused.cpu().numpy()) <= 1e-2
+
+
+@pytest.mark.parametrize("mode", ["dot", "add"])
+@pytest.mark.parametrize("F,H", [(64, 1), (32, 4), (128, 2)])
+def test_fused_gat_tf32_vs_fp64(cuda, mode, F, H):
+    """fp32 X' on TF32 tensor cores (3xTF32 logits and aggregation): within
+    1e-4 of FP64, split windows (partial merge) included."""
+    from att_gb300 import gat
+    n = 1500
+    rp, col = _graph(n, 40, 1.9, seed=9, hub=True)
+    G = gat.GATGraph(rp, col, parts_per_chunk=2)
+    assert G.n_multi > 0
+    g = torch.Generator().manual_seed(F * H)
+    Xp = (torch.rand(n, H * F, generator=g) * 2 - 1) * (0.6 if mode == "dot" else 1.0)
+    X3 = Xp.view(n, H, F).permute(1, 0, 2).double().numpy()
+    rpn, coln = rp.numpy(), col.numpy()
+    if mode == "dot":
+        out, rmax, rsum = G.attention(Xp.cuda(), n_heads=H, mode=gat.MODE_DOT)
+        ref = oracle.gat_dot_layer_fp64(rpn, coln, X3, n)
+    else:
+        a0 = (torch.rand(H, F, generator=g) - 0.5)
+        a1 = (torch.rand(H, F, generator=g) - 0.5)
+        s0 = torch.einsum("hmf,hf->hm", torch.from_numpy(X3), a0.double()).float()
+        s1 = torch.einsum("hmf,hf->hm", torch.from_numpy(X3), a1.double()).float()
+        out, rmax, rsum = G.attention(Xp.cuda(), n_heads=H, mode=gat.MODE_ADD, s0=s0.cuda(),
+                                      s1=s1.cuda())
+        ref = oracle.gat_layer_fp64(rpn, coln, X3, a0.numpy()[:, None, :], a1.numpy()[:, None, :], n)
+    got = out.view(n, H, F).permute(1, 0, 2).cpu().numpy()
+    err = oracle.rel_err(got, ref)
+    assert err <= 1e-4, err
+    assert torch.isfinite(rmax[:, :n]).all() and (rsum[:, :n] >= 1.0 - 1e-3).all()
