@@ -49,6 +49,18 @@ MEASURED_TRAFFIC = {
     ("spmm_products_fp16", 1.0): {
         "bytes": 9950022656 + 1406364928, "kernel": "k_spmm16<__half, 8, 64, 8, 3, int>",
         "ncu_ms": 2.188, "note": "read 9.95 GB + write 1.41 GB; X rows of hub columns hit L2"},
+    ("spmm_products_bf16", 1.0): {
+        "bytes": 9952612096 + 1407312128, "kernel": "k_spmm16<__nv_bfloat16, 8, 64, 8, 2, int, 1>",
+        "ncu_ms": 2.220, "note": "read 9.95 GB + write 1.41 GB; the captured launch was the "
+                                 "autotuner's 2-stage candidate (ring depth does not change "
+                                 "the bytes)"},
+    ("spmm_products_fp8", 1.0): {
+        "bytes": 5507631872 + 1378852096, "kernel": "k_spmm_fp8r<8, 128, 8, int, 1>",
+        "ncu_ms": 2.018, "note": "read 5.51 GB + write 1.38 GB (fp16 kernel: 11.36 GB)"},
+    ("gat_reddit_fp16", 1.0): {
+        "bytes": 591916800 + 229291008, "kernel": "k_gat_fused<__half, 64, 0, 0, int>",
+        "ncu_ms": 2.765, "note": "read 0.59 GB + write 0.23 GB: X' (30 MB) is L2-resident, "
+                                 "the gathers are served by L2"},
 }
 METRIC = "SpMM/SDDMM HBM GB/s (% roofline); GAT step ms; serve p50/p99 vs plain"
 
