@@ -136,6 +136,84 @@ __device__ __forceinline__ bool window_range(const int32_t *rowptr, int64_t w, i
 }
 
 // ---- plan: distinct sorted columns per window ------------------------------
+// Windows of at most kWarpCap edges (most windows of a sparse graph): one warp
+// each, a bitonic sort of the window's column ids in the warp's own slice of
+// shared memory (warp-synchronous, no block barriers), then de-duplication
+// and a warp scan to compact.
+constexpr int kWarpCap = 256;
+constexpr int kWarpSortWarps = 8;
+
+__global__ void __launch_bounds__(kWarpSortWarps * 32) k_unique_warp(
+    const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col, int64_t n_win,
+    int window, int64_t nnz, int64_t n_cols, Workspace ws) {
+    __shared__ int keys_all[kWarpSortWarps][kWarpCap];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int *keys = keys_all[wib];
+    const int64_t nwarps = (int64_t)gridDim.x * kWarpSortWarps;
+    for (int64_t w = (int64_t)blockIdx.x * kWarpSortWarps + wib; w < n_win; w += nwarps) {
+        int64_t b0, b1;
+        window_range(rowptr, w, window, nnz, &b0, &b1, ws.flags);
+        const int64_t E = b1 - b0;
+        if (E > kWarpCap) continue;  // k_unique_small / k_unique_large
+        int n = 32;
+        while (n < E) n <<= 1;
+        for (int t = lane; t < n; t += 32) {
+            int c = INT32_MAX;
+            if (t < E) {
+                c = col[b0 + t];
+                if (c < 0 || c >= n_cols) {
+                    atomicOr(ws.flags, FLAG_BAD_COL);
+                    c = INT32_MAX;
+                }
+            }
+            keys[t] = c;
+        }
+        __syncwarp();
+        for (int k = 2; k <= n; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int t = lane; t < (n >> 1); t += 32) {
+                    const int i = 2 * t - (t & (j - 1)), l = i + j;  // pair (i, i + j)
+                    const int a = keys[i], b = keys[l];
+                    if ((a > b) == ((i & k) == 0)) {
+                        keys[i] = b;
+                        keys[l] = a;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // de-duplicate: lane owns n / 32 consecutive sorted keys
+        const int per = n >> 5, base = lane * per;
+        int cnt = 0;
+        for (int q = 0; q < per; ++q) {
+            const int kk = base + q;
+            if (kk < E) {
+                const int v = keys[kk];
+                if (v != INT32_MAX && (kk == 0 || keys[kk - 1] != v)) cnt++;
+            }
+        }
+        int x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, x, 31);
+        int pos = x - cnt;
+        for (int q = 0; q < per; ++q) {
+            const int kk = base + q;
+            if (kk < E) {
+                const int v = keys[kk];
+                if (v != INT32_MAX && (kk == 0 || keys[kk - 1] != v)) ws.ucols[b0 + pos++] = v;
+            }
+        }
+        if (lane == 0) ws.ucount[w] = total;
+        __syncwarp();
+    }
+}
+
+// Windows of kWarpCap+1 .. kSmallCap edges: one CTA each, bitonic sort in
+// shared memory across the block.
 __global__ void __launch_bounds__(kSmallThreads) k_unique_small(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col, int64_t n_win,
     int window, int64_t nnz, int64_t n_cols, Workspace ws) {
@@ -145,7 +223,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_unique_small(
         int64_t b0, b1;
         window_range(rowptr, w, window, nnz, &b0, &b1, ws.flags);
         int64_t E = b1 - b0;
-        if (E > kSmallCap) continue;  // handled by k_unique_large
+        if (E > kSmallCap || E <= kWarpCap) continue;  // k_unique_large / k_unique_warp
         int n = 1;
         while (n < E) n <<= 1;
         for (int t = threadIdx.x; t < n; t += kSmallThreads) {
@@ -164,7 +242,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_unique_small(
         for (int k = 2; k <= n; k <<= 1) {
             for (int j = k >> 1; j > 0; j >>= 1) {
                 for (int t = threadIdx.x; t < (n >> 1); t += kSmallThreads) {
-                    int i = (t / j) * 2 * j + (t % j);
+                    int i = 2 * t - (t & (j - 1));  // (t / j) * 2j + t % j, j a power of two
                     int l = i + j;
                     int a = keys[i], b = keys[l];
                     bool up = (i & k) == 0;
@@ -507,6 +585,11 @@ static int plan_enqueue(const int32_t *rowptr, const int32_t *col, int64_t n_row
         ATT_CUDA(cudaMemsetAsync(ws.ucount, 0, (size_t)nw * 4, st), "memset ucount");
         int sms = sm_count();
         int64_t g_small = nw < (int64_t)sms * 32 ? nw : (int64_t)sms * 32;
+        const int64_t g_warp0 = (nw + kWarpSortWarps - 1) / kWarpSortWarps;
+        const int64_t g_warp = g_warp0 < (int64_t)sms * 16 ? g_warp0 : (int64_t)sms * 16;
+        k_unique_warp<<<(unsigned)g_warp, kWarpSortWarps * 32, 0, st>>>(rowptr, col, nw, window,
+                                                                          nnz, n_cols, ws);
+        ATT_CUDA(cudaGetLastError(), "k_unique_warp");
         k_unique_small<<<(unsigned)g_small, kSmallThreads, 0, st>>>(rowptr, col, nw, window, nnz,
                                                                      n_cols, ws);
         int64_t g_large = nw < ws.n_bitmap_ctas ? nw : ws.n_bitmap_ctas;
