@@ -442,13 +442,16 @@ class Server:
     pinned memory) -> ready for layer 1 -> [tick] -> ready for layer 2 ->
     [tick] -> download (copy stream) -> done."""
 
-    def __init__(self, model, budget=120e9, max_active=64, workers=8, use_graph=True,
+    def __init__(self, model, budget=120e9, max_active=64, workers=2, use_graph=True,
                  keep_outputs=True, max_inflight_ticks=2, group_parts=GROUP_PARTS,
                  direct_output=True, checksum=False):
         require_cuda()
         self.model = model
         self.adm = Admission(budget, max_active)
-        self.workers = workers  # preparation streams (requests converting at once)
+        # preparation streams (requests converting at once); two measured the
+        # lowest p99 on the 32-graph Poisson trace (fewer conversions
+        # competing with each other and with the ticks)
+        self.workers = workers
         self.group_parts = group_parts
         # preparation on default-priority streams; ticks and result copies on
         # high-priority streams, so requests already on the device are not

@@ -934,7 +934,7 @@ def run_serving(args):
     count = max(args.steps, 20)
     group_parts, group_ms = _tune_serving_groups(pool, model)
     reqs = serving.make_requests(pool, SERVE_RATE, count, SERVE_SEED)
-    srv = serving.Server(model, budget=120e9, max_active=64, workers=8, keep_outputs=False,
+    srv = serving.Server(model, budget=120e9, max_active=64, workers=2, keep_outputs=False,
                          group_parts=group_parts)
     # warm-up to the steady state of a running server: a real-time trace of
     # another seed through both paths (the caching device and pinned-host
@@ -974,7 +974,7 @@ def run_serving(args):
     # split windows with atomics, so they differ by fp32 rounding only)
     vr = [serving.Request(r.rid, 0.0, r.rowptr, r.col, r.X, r.n, r.nnz) for r in reqs[:48]]
     vp = [serving.Request(r.rid, 0.0, r.rowptr, r.col, r.X, r.n, r.nnz) for r in reqs[:48]]
-    serving.Server(model, budget=120e9, max_active=64, workers=8,
+    serving.Server(model, budget=120e9, max_active=64, workers=2,
                    group_parts=group_parts).run(vr, realtime=False)
     serving.serve_one_by_one(vp, model, realtime=False)
     agree = max(float((a.out - b.out).abs().max() / b.out.abs().max().clamp_min(1e-30))
@@ -995,7 +995,7 @@ def run_serving(args):
                        "seed": SERVE_SEED, "graph_pool": len(pool),
                        "nodes": "log-uniform [%d, %d]" % (min(p[3] for p in pool), max(p[3] for p in pool)),
                        "mean_degree": "uniform [5, 50]", "model": "2-layer GCN, hidden 128, fp16",
-                       "hbm_budget_bytes": 120e9, "max_active": 64, "workers": 8,
+                       "hbm_budget_bytes": 120e9, "max_active": 64, "workers": 2,
                        "step": "one request (arrival -> result in pinned host memory)",
                        "l2": "graphs and features change every request; no flush"},
             "serve": {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
