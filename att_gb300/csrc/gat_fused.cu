@@ -675,6 +675,10 @@ struct GatBwdArgs {
     int32_t *err;
 };
 
+// the backward's ring depth: 2 stages leave room for 6 CTAs per SM where 3
+// stages allowed 4 (the kernel is latency-bound: warps matter more than depth)
+constexpr int kBStages = 2;
+
 template <typename T, int F, bool SPLIT>
 struct BCfg {
     static constexpr int XROW = F * 2;
@@ -683,7 +687,7 @@ struct BCfg {
     static constexpr int MSTAGE = 16;
     static constexpr int CSTAGE = 5 * 64;  // s0, m, l, c and the ids of the 16 columns
     static constexpr int STAGE = XSTAGE + MSTAGE + CSTAGE;
-    static constexpr int WARP_SMEM = kGStages * STAGE;
+    static constexpr int WARP_SMEM = kBStages * STAGE;
     static constexpr int SMEM = kGWarps * WARP_SMEM;
     static constexpr int CPR = XROW / 16;
     static constexpr int PASSES = (16 * CPR + 31) / 32;
@@ -784,7 +788,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
     p_load();
     p_fetch();
 #pragma unroll
-    for (int s = 0; s < kGStages - 1; ++s) {
+    for (int s = 0; s < kBStages - 1; ++s) {
         if (p_item < n_items) {
             issue(s);
             p_advance();
@@ -799,7 +803,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         const int c = gid + 8 * (u >> 1), r = 2 * tig + (u & 1);
         mbit[u] = (c & ~wmask) * kW + r * A.wide + (c & wmask);
     }
-    int cstage = 0, pstage = kGStages - 1;
+    int cstage = 0, pstage = kBStages - 1;
     for (IT c_item = (IT)blockIdx.x * kGWarps + warp; c_item < n_items; c_item += stride) {
         const IT part = c_item / H;
         const IT h = c_item - part * H;
@@ -832,7 +836,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
         for (int j = 0; j < C::MT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
 
         for (int step = 0; step < nsteps; ++step) {
-            cp_async_wait<kGStages - 2>();
+            cp_async_wait<kBStages - 2>();
             __syncwarp();
             const uint32_t xs = sbase + cstage * C::STAGE;
             const uint32_t *mw = (const uint32_t *)(sgen + cstage * C::STAGE + C::XSTAGE);
@@ -913,8 +917,8 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
                 p_advance();
             }
             cp_async_commit();
-            cstage = cstage + 1 == kGStages ? 0 : cstage + 1;
-            pstage = pstage + 1 == kGStages ? 0 : pstage + 1;
+            cstage = cstage + 1 == kBStages ? 0 : cstage + 1;
+            pstage = pstage + 1 == kBStages ? 0 : pstage + 1;
         }
 #pragma unroll
         for (int j = 0; j < C::MT; ++j)
