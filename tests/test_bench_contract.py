@@ -39,3 +39,21 @@ def test_reference_arm_time_metric_workload():
              "--warmup", "3", "--scale", "0.02")
     assert d["impl"] == "reference" and d["unit"] == "ms" and d["higher_is_better"] is False
     assert d["value"] > 0
+
+
+def test_reference_arm_serving_workload():
+    d = _run("--impl", "reference", "--workload", "serve_gcn_fp16", "--steps", "1",
+             "--warmup", "3", "--scale", "0.01")
+    assert d["impl"] == "reference" and d["unit"] == "ms" and d["higher_is_better"] is False
+    assert d["value"] > 0 and d["config"]["workload"] == "serve_gcn_fp16"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_other_ranks_stay_silent():
+    """Under torchrun only rank 0 runs and prints the reference line."""
+    env = dict(os.environ, RANK="1", LOCAL_RANK="1", WORLD_SIZE="2")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "3", "--scale", "0.01"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert not [l for l in out.stdout.splitlines() if l.startswith("{")]
