@@ -378,3 +378,111 @@ def rel_err_fro(got, ref):
     ref = np.asarray(ref, dtype=np.float64)
     d = np.linalg.norm(ref)
     return float(np.linalg.norm(got - ref) / d) if d > 0 else 0.0
+
+
+# --------------------------------------------------------------------------
+# Row-sampled FP64 restatements (full-size graphs: only the sampled rows and
+# the neighbours they read are evaluated)
+# --------------------------------------------------------------------------
+
+def sub_csr(rowptr, col, rows):
+    """CSR restricted to `rows` (in the given order): (rowptr_sub int64,
+    col_sub int64, edge ids int64 into the full CSR)."""
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    rows = np.asarray(rows, dtype=np.int64)
+    starts, ends = rowptr[rows], rowptr[rows + 1]
+    lens = ends - starts
+    rp = np.zeros(rows.shape[0] + 1, dtype=np.int64)
+    np.cumsum(lens, out=rp[1:])
+    eid = np.repeat(starts - rp[:-1], lens) + np.arange(rp[-1], dtype=np.int64)
+    return rp, np.asarray(col, dtype=np.int64)[eid], eid
+
+
+def sample_rows(rowptr, n_rows, n_random, n_top, seed, window=8):
+    """Sorted unique row ids: `n_random` seeded random rows plus every row of
+    the windows that hold the `n_top` longest rows (the hub windows, whose
+    parts split the most)."""
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    lens = np.diff(rowptr)[:n_rows]
+    rng = np.random.default_rng(seed)
+    pick = [rng.choice(n_rows, size=min(n_random, n_rows), replace=False)]
+    top = np.argsort(lens, kind="stable")[::-1][:n_top]
+    for r in top:
+        w0 = (r // window) * window
+        pick.append(np.arange(w0, min(w0 + window, n_rows)))
+    return np.unique(np.concatenate(pick))
+
+
+def spmm_rows_fp64(rowptr, col, vals, X, rows):
+    """(A X)[rows] in FP64; `vals` are the per-edge values of the full CSR."""
+    rp, c, eid = sub_csr(rowptr, col, rows)
+    return spmm_csr_fp64(rp, c, np.asarray(vals)[eid], X)
+
+
+def gat_dot_rows_fp64(rowptr, col, Xp, rows, slope=0.2):
+    """Dot-logit GAT layer (one head) for `rows`: e_ij = Xp_i . Xp_j on the
+    edges, LeakyReLU, row softmax, sum_j p_ij Xp_j.  Xp [N, F]."""
+    rows = np.asarray(rows, dtype=np.int64)
+    rp, c, _ = sub_csr(rowptr, col, rows)
+    X = np.asarray(Xp, dtype=np.float64)
+    lens = np.diff(rp)
+    out = np.zeros((len(rows), X.shape[1]))
+    nz = np.nonzero(lens)[0]
+    if nz.size == 0:
+        return out
+    seg = np.repeat(np.arange(len(rows)), lens)
+    Xc = X[c]
+    e = np.einsum("ef,ef->e", X[rows[seg]], Xc)
+    e = np.where(e > 0, e, slope * e)
+    starts = rp[:-1][nz]  # segments are contiguous and in row order
+    m = np.maximum.reduceat(e, starts)
+    mm = np.zeros(len(rows))
+    mm[nz] = m
+    pe = np.exp(e - mm[seg])
+    l = np.add.reduceat(pe, starts)
+    acc = np.add.reduceat(pe[:, None] * Xc, starts, axis=0)
+    out[nz] = acc / l[:, None]
+    return out
+
+
+def gat_add_rows_torch(rowptr, col, Xp, a0, a1, rows, slope=0.2):
+    """Differentiable FP64 restatement of the additive multi-head GAT
+    aggregation (end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198, no
+    dropout) for `rows` only: Xp [N, H*F] (full, requires_grad allowed),
+    a0 / a1 [H, F] -> [len(rows), H*F].  Gradients flow to every Xp row the
+    sampled rows read."""
+    import torch
+    rp, c, _ = sub_csr(rowptr, col, rows)
+    H, F = a0.shape
+    rows_t = torch.as_tensor(np.asarray(rows, dtype=np.int64))
+    c_t = torch.as_tensor(c)
+    seg = torch.repeat_interleave(torch.arange(len(rows)), torch.as_tensor(np.diff(rp)))
+    X3 = Xp.view(Xp.shape[0], H, F)
+    s0 = (X3[rows_t] * a0[None]).sum(-1)
+    Xc = X3[c_t]
+    s1 = (Xc * a1[None]).sum(-1)
+    e = torch.nn.functional.leaky_relu(s0[seg] + s1, slope)
+    m = torch.full((len(rows), H), float("-inf"), dtype=e.dtype).scatter_reduce(
+        0, seg[:, None].expand(-1, H), e, "amax").detach()
+    ex = torch.exp(e - m[seg])
+    l = torch.zeros(len(rows), H, dtype=e.dtype).index_add(0, seg, ex)
+    p = ex / l[seg]
+    out = torch.zeros(len(rows), H, F, dtype=e.dtype).index_add(0, seg, p[:, :, None] * Xc)
+    return out.reshape(len(rows), H * F)
+
+
+def gcn2_fp64(rowptr, col, vals, X, W1, W2, n_out):
+    """2-layer GCN inference Y = A relu(A X W1) W2 in FP64 on the host (torch
+    CSR, all host threads); A from per-edge values (the GCN layer composition of
+    end2end_ori/gcn_final/mgat_csr/mgat_conv.py:27-54 with ReLU between)."""
+    import torch
+    rowptr = torch.as_tensor(np.asarray(rowptr, dtype=np.int64))
+    A = torch.sparse_csr_tensor(rowptr, torch.as_tensor(np.asarray(col, dtype=np.int64)),
+                                torch.as_tensor(np.asarray(vals, dtype=np.float64)),
+                                size=(rowptr.numel() - 1, X.shape[0]))
+    X = torch.as_tensor(np.asarray(X, dtype=np.float64))
+    W1 = torch.as_tensor(np.asarray(W1, dtype=np.float64))
+    W2 = torch.as_tensor(np.asarray(W2, dtype=np.float64))
+    H = torch.relu(torch.sparse.mm(A, X @ W1))
+    Y = torch.sparse.mm(A, H[: X.shape[0]] @ W2)
+    return Y[:n_out].numpy()

@@ -144,3 +144,54 @@ def test_gat_oracles_match_dense_restatement():
     add = dense((X @ a0.transpose(0, 2, 1)) + (X @ a1.transpose(0, 2, 1)).transpose(0, 2, 1))
     assert np.allclose(oracle.gat_dot_layer_fp64(rp, col, X, n), dot, rtol=0, atol=1e-12)
     assert np.allclose(oracle.gat_layer_fp64(rp, col, X, a0, a1, n), add, rtol=0, atol=1e-12)
+
+
+def _small_graph(seed=3, n=300):
+    from att_gb300 import graphs
+    import torch
+    rp, col = graphs.chung_lu(n, 9, 2.1, seed=seed)
+    return rp.numpy(), col.numpy()
+
+
+def test_row_sampled_restatements_match_whole_graph():
+    """sub_csr / sample_rows and the row-sampled FP64 functions agree with the
+    whole-graph restatements on the sampled rows."""
+    import torch
+    rp, col = _small_graph()
+    n = rp.shape[0] - 1
+    rows = oracle.sample_rows(rp, n, 40, 3, seed=1)
+    lens = np.diff(rp)
+    top = np.argsort(lens)[::-1][:3]
+    for r in top:  # every row of each hub window is in the sample
+        w0 = r // 8 * 8
+        assert set(range(w0, min(w0 + 8, n))) <= set(rows.tolist())
+    srp, scol, eid = oracle.sub_csr(rp, col, rows)
+    assert np.array_equal(np.diff(srp), lens[rows])
+    assert np.array_equal(scol, col[eid])
+    rng = np.random.default_rng(0)
+    X = rng.uniform(-1, 1, (n, 16))
+    vals = rng.uniform(0, 1, col.shape[0])
+    full = oracle.spmm_csr_fp64(rp, col, vals, X)
+    assert np.allclose(oracle.spmm_rows_fp64(rp, col, vals, X, rows), full[rows], atol=1e-12)
+    gat_full = oracle.gat_dot_layer_fp64(rp, col, X[None], n)[0]
+    assert np.allclose(oracle.gat_dot_rows_fp64(rp, col, X, rows), gat_full[rows], atol=1e-12)
+    H, F = 2, 8
+    Xp = torch.from_numpy(rng.uniform(-1, 1, (n, H * F)))
+    a0 = torch.from_numpy(rng.uniform(-0.5, 0.5, (H, F)))
+    a1 = torch.from_numpy(rng.uniform(-0.5, 0.5, (H, F)))
+    whole = oracle.gat_add_layer_torch(rp, col, Xp, a0, a1)
+    part = oracle.gat_add_rows_torch(rp, col, Xp, a0, a1, rows)
+    assert torch.allclose(part, whole[torch.from_numpy(rows)], atol=1e-12)
+
+
+def test_gcn2_restatement_is_two_layers_of_spmm():
+    rp, col = _small_graph(seed=5, n=200)
+    n = rp.shape[0] - 1
+    rng = np.random.default_rng(1)
+    X = rng.uniform(-1, 1, (n, 8))
+    W1 = rng.uniform(-1, 1, (8, 6))
+    W2 = rng.uniform(-1, 1, (6, 4))
+    vals = rng.uniform(0, 1, col.shape[0])
+    h = np.maximum(oracle.spmm_csr_fp64(rp, col, vals, X @ W1), 0)
+    want = oracle.spmm_csr_fp64(rp, col, vals, h @ W2)
+    assert np.allclose(oracle.gcn2_fp64(rp, col, vals, X, W1, W2, n), want, atol=1e-12)
