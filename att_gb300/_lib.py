@@ -24,6 +24,7 @@ _SIGNATURES = {
     "att_last_error": (ctypes.c_char_p, []),
     "att_version": (_c_int, []),
     "att_set_option": (_c_int, [ctypes.c_char_p, _c_int]),
+    "att_set_thread_option": (_c_int, [ctypes.c_char_p, _c_int]),
     "att_get_option": (_c_int, [ctypes.c_char_p, ctypes.POINTER(_c_int)]),
     "att_block_workspace_bytes": (_c_sz, [_c_i64, _c_i64, _c_i64, _c_int]),
     "att_block_plan": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int, _c_int,

@@ -73,7 +73,17 @@ _default = Tuner()
 
 
 def _set(key, value):
-    _lib.call("att_set_option", key.encode(), int(value))
+    """Override a launch-shape knob for the calling thread only."""
+    _lib.call("att_set_thread_option", key.encode(), int(value))
+
+
+SHAPE_KNOBS = ("spmm_fc", "spmm_stages", "spmm_fp8", "spmm_tf32")
+
+
+def clear_shape():
+    """Return the calling thread to the process-wide launch-shape defaults."""
+    for k in SHAPE_KNOBS:
+        _set(k, -1)
 
 
 def spmm_candidates(x_dtype, F):
@@ -88,7 +98,10 @@ def spmm_candidates(x_dtype, F):
     return []
 
 
-def _apply_spmm(c):
+def apply_shape(c):
+    """Set the calling thread's att_spmm launch shape to candidate `c`."""
+    if c is None:
+        return
     if c[0] == "spmm":
         _set("spmm_fc", c[1])
         _set("spmm_stages", c[2])
@@ -100,9 +113,11 @@ def _apply_spmm(c):
 
 def tune_spmm(fmt, X, m_out, x_scale=None, out=None, val=None, tuner=None):
     """Time att_spmm's launch shapes on this format and features (block
-    values `val`, default the format's own), set the fastest as the
-    process-wide options, and return (choice, {choice: ms}).  Shapes with
-    nothing to tune (fp32 features with F <= 32) return (None, {})."""
+    values `val`, default the format's own) and return (choice, {choice:
+    ms}).  Candidates are applied to the calling thread only and the thread
+    is returned to the defaults afterwards: pass the choice to
+    ``ops.spmm(..., shape=choice)`` for the calls it was tuned for.  Shapes
+    with nothing to tune (fp32 features with F <= 32) return (None, {})."""
     tuner = tuner or _default
     F = int(X.shape[1])
     cands = spmm_candidates(X.dtype, F)
@@ -117,7 +132,10 @@ def tune_spmm(fmt, X, m_out, x_scale=None, out=None, val=None, tuner=None):
     def run():
         ops.spmm(fmt.rowptr, fmt.col, vals, fmt.window_of_part, fmt.atomic, X, m_out,
                  window=fmt.window, wide=fmt.wide, out=Y, x_scale=x_scale)
-    return tuner.best(key, cands, _apply_spmm, run)
+    try:
+        return tuner.best(key, cands, apply_shape, run)
+    finally:
+        clear_shape()
 
 
 def tune_group_parts(requests, candidates=(1, 2, 4, 8), tuner=None):

@@ -30,6 +30,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <mutex>
 #include <string.h>
 #include <type_traits>
@@ -1934,23 +1935,48 @@ int launch16_tma(const int32_t *rowptr, const int32_t *col, const void *val, con
 
 constexpr int kTmaStages = 5;
 
-// Row-gather mechanism of the 16-bit kernel: 0 = cp.async (default), 1 = TMA
-// tile::gather4, 2 = cp.async.bulk per row.  Set through
-// att_set_option("spmm_gather", ...).
-int g_spmm_gather = 0;
-// Ring depth of the 16-bit cp.async kernel (2, 3, 4) and features per work
-// item for F > 64 (64 or 128); att_set_option("spmm_stages" / "spmm_fc").
-// Measured on the 2.45M-node graph (F = 128): throughput follows resident
-// warps per SM, not the depth of each warp's ring -- 64 features x 3 stages
-// (3.03 ms) beats 128 x 4 (4.24 ms) and 128 x 6 (5.92 ms).
-int g_spmm_stages = 3;
-int g_spmm_fc = 64;
-// FP8 kernel: 1 = A fragments dequantized in registers (k_spmm_fp8r, 128
-// features per item when F > 64), 0 = through an fp16 shared tile
-// (k_spmm_fp8); att_set_option("spmm_fp8", ...).
-int g_spmm_fp8 = 1;
-// fp32-feature (3xTF32) kernel shape; att_set_option("spmm_tf32", 0..3)
-int g_spmm_tf32 = 0;
+// Launch-shape options of att_spmm.  Each has a process-wide default
+// (att_set_option, atomic) and a per-thread override (att_set_thread_option,
+// -1 = follow the default), so a caller -- or the autotuner -- can pick the
+// shape of its own calls without changing the shape of calls made by other
+// threads.
+//  * spmm_gather: row-gather mechanism of the 16-bit kernel, 0 = cp.async
+//    (default), 1 = TMA tile::gather4, 2 = cp.async.bulk per row.
+//  * spmm_stages / spmm_fc: ring depth of the 16-bit cp.async kernel (2, 3,
+//    4) and features per work item for F > 64 (64 or 128).  Measured on the
+//    2.45M-node graph (F = 128): throughput follows resident warps per SM,
+//    not the depth of each warp's ring.
+//  * spmm_fp8: 1 = A fragments dequantized in registers (k_spmm_fp8r, 128
+//    features per item when F > 64), 0 = through an fp16 shared tile
+//    (k_spmm_fp8).
+//  * spmm_tf32: fp32-feature (3xTF32) kernel shape 0..3.
+enum SpmmOpt { kOptGather = 0, kOptStages, kOptFc, kOptFp8, kOptTf32, kNumOpts };
+const char *const kOptNames[kNumOpts] = {"spmm_gather", "spmm_stages", "spmm_fc", "spmm_fp8",
+                                         "spmm_tf32"};
+std::atomic<int> g_opt[kNumOpts] = {{0}, {3}, {64}, {1}, {0}};
+thread_local int t_opt[kNumOpts] = {-1, -1, -1, -1, -1};
+
+inline int opt(SpmmOpt i) {
+    const int v = t_opt[i];
+    return v >= 0 ? v : g_opt[i].load(std::memory_order_relaxed);
+}
+
+int opt_index(const char *key) {
+    for (int i = 0; i < kNumOpts; ++i)
+        if (strcmp(key, kOptNames[i]) == 0) return i;
+    return -1;
+}
+
+bool opt_valid(int i, int v) {
+    switch (i) {
+        case kOptGather: return v >= 0 && v <= 2;
+        case kOptStages: return v == 2 || v == 3 || v == 4;
+        case kOptFc: return v == 64 || v == 128;
+        case kOptFp8: return v == 0 || v == 1;
+        case kOptTf32: return v >= 0 && v <= 3;
+    }
+    return false;
+}
 
 template <int W, int FC, int WIDE>
 int launch_fp8(const int32_t *rowptr, const int32_t *col, const void *val, const int32_t *win,
@@ -2013,7 +2039,7 @@ int dispatch_fc16(const int32_t *rowptr, const int32_t *col, const void *val, co
                   cudaStream_t st) {
     // TMA row gathers for F >= 64 (the tensor map's 64-feature box fits); the
     // cp.async kernel for narrower features or an X without rows
-    if (g_spmm_gather == 1 && F >= 64 && n_x > 0 && n_x < INT32_MAX &&
+    if (opt(kOptGather) == 1 && F >= 64 && n_x > 0 && n_x < INT32_MAX &&
         tensor_map_encoder() != nullptr) {
         if (F <= 64)
             return launch16_tma<T, W, 64, WIDE, kTmaStages>(rowptr, col, val, win, atomic, n_parts,
@@ -2025,20 +2051,20 @@ int dispatch_fc16(const int32_t *rowptr, const int32_t *col, const void *val, co
         return launch16<T, W, 32, WIDE>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
                                         m_out, ldy, err, st);
     if constexpr (W == 8 && WIDE == 8) {
-        if (g_spmm_gather == 2 && (F <= 64 || g_spmm_fc == 64))
+        if (opt(kOptGather) == 2 && (F <= 64 || opt(kOptFc) == 64))
             return launch16_bulk<T, 3>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, Y,
                                        m_out, ldy, err, st);
     }
 #define ATT_L16S(FCv, Sv)                                                                       \
     return launch16<T, W, FCv, WIDE, Sv>(rowptr, col, val, win, atomic, n_parts, X, n_x, F, ldx, \
                                          Y, m_out, ldy, err, st)
-    if (F <= 64 || g_spmm_fc == 64) {
-        if (g_spmm_stages == 2) ATT_L16S(64, 2);
-        if (g_spmm_stages == 4) ATT_L16S(64, 4);
+    if (F <= 64 || opt(kOptFc) == 64) {
+        if (opt(kOptStages) == 2) ATT_L16S(64, 2);
+        if (opt(kOptStages) == 4) ATT_L16S(64, 4);
         ATT_L16S(64, 3);
     }
-    if (g_spmm_stages == 2) ATT_L16S(128, 2);
-    if (g_spmm_stages == 4) ATT_L16S(128, 4);
+    if (opt(kOptStages) == 2) ATT_L16S(128, 2);
+    if (opt(kOptStages) == 4) ATT_L16S(128, 4);
     ATT_L16S(128, 3);
 #undef ATT_L16S
 }
@@ -2053,11 +2079,11 @@ int dispatch_fc32(const int32_t *rowptr, const int32_t *col, const void *val, co
                                          Y, m_out, ldy, err, st)
     // shapes (features per item x ring depth): 0 = 64 x 4, 1 = 32 x 3,
     // 2 = 32 x 4, 3 = 64 x 2 (F <= 32 always takes 32-feature items)
-    if (F <= 32 || g_spmm_tf32 == 1 || g_spmm_tf32 == 2) {
-        if (g_spmm_tf32 == 1) ATT_LTF(32, 3);
+    if (F <= 32 || opt(kOptTf32) == 1 || opt(kOptTf32) == 2) {
+        if (opt(kOptTf32) == 1) ATT_LTF(32, 3);
         ATT_LTF(32, 4);
     }
-    if (g_spmm_tf32 == 3) ATT_LTF(64, 2);
+    if (opt(kOptTf32) == 3) ATT_LTF(64, 2);
     ATT_LTF(64, 4);
 #undef ATT_LTF
 }
@@ -2146,7 +2172,7 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
 #define ATT_F8R(Wv, FCv, WIDEv)                                                                \
     return launch_fp8r<Wv, FCv, WIDEv>(rowptr, col, val, window_of_part, atomic, n_parts, X,   \
                                        x_scale, n_x_rows, F, ldx, Y, m_out, ldy, err_flag, st)
-        if (g_spmm_fp8 == 1) {
+        if (opt(kOptFp8) == 1) {
             if (F > 64) {
                 if (window == 8) { if (wide == 8) ATT_F8R(8, 128, 8); ATT_F8R(8, 128, 16); }
                 if (wide == 8) ATT_F8R(16, 128, 8);
@@ -2174,61 +2200,32 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
 extern "C" int att_set_option(const char *key, int value) {
     clear_error();
     ATT_CHECK(key != nullptr, ATT_ERR_INVALID, "null option name");
-    if (strcmp(key, "spmm_gather") == 0) {
-        ATT_CHECK(value >= 0 && value <= 2, ATT_ERR_INVALID, "spmm_gather must be 0, 1 or 2");
-        g_spmm_gather = value;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_stages") == 0) {
-        ATT_CHECK(value == 2 || value == 3 || value == 4, ATT_ERR_INVALID,
-                  "spmm_stages must be 2, 3 or 4");
-        g_spmm_stages = value;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_fc") == 0) {
-        ATT_CHECK(value == 64 || value == 128, ATT_ERR_INVALID, "spmm_fc must be 64 or 128");
-        g_spmm_fc = value;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_tf32") == 0) {
-        ATT_CHECK(value >= 0 && value <= 3, ATT_ERR_INVALID, "spmm_tf32 must be 0..3");
-        g_spmm_tf32 = value;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_fp8") == 0) {
-        ATT_CHECK(value == 0 || value == 1, ATT_ERR_INVALID, "spmm_fp8 must be 0 or 1");
-        g_spmm_fp8 = value;
-        return ATT_OK;
-    }
-    set_error("unknown option '%s'", key);
-    return ATT_ERR_INVALID;
+    const int i = opt_index(key);
+    ATT_CHECK(i >= 0, ATT_ERR_INVALID, "unknown option '%s'", key);
+    ATT_CHECK(opt_valid(i, value), ATT_ERR_INVALID, "invalid value %d for option '%s'", value,
+              key);
+    g_opt[i].store(value, std::memory_order_relaxed);
+    return ATT_OK;
+}
+
+extern "C" int att_set_thread_option(const char *key, int value) {
+    clear_error();
+    ATT_CHECK(key != nullptr, ATT_ERR_INVALID, "null option name");
+    const int i = opt_index(key);
+    ATT_CHECK(i >= 0, ATT_ERR_INVALID, "unknown option '%s'", key);
+    ATT_CHECK(value == -1 || opt_valid(i, value), ATT_ERR_INVALID,
+              "invalid value %d for option '%s'", value, key);
+    t_opt[i] = value;
+    return ATT_OK;
 }
 
 extern "C" int att_get_option(const char *key, int *value) {
     clear_error();
     ATT_CHECK(key != nullptr && value != nullptr, ATT_ERR_INVALID, "null argument");
-    if (strcmp(key, "spmm_gather") == 0) {
-        *value = g_spmm_gather;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_stages") == 0) {
-        *value = g_spmm_stages;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_tf32") == 0) {
-        *value = g_spmm_tf32;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_fp8") == 0) {
-        *value = g_spmm_fp8;
-        return ATT_OK;
-    }
-    if (strcmp(key, "spmm_fc") == 0) {
-        *value = g_spmm_fc;
-        return ATT_OK;
-    }
-    set_error("unknown option '%s'", key);
-    return ATT_ERR_INVALID;
+    const int i = opt_index(key);
+    ATT_CHECK(i >= 0, ATT_ERR_INVALID, "unknown option '%s'", key);
+    *value = opt((SpmmOpt)i);
+    return ATT_OK;
 }
 
 extern "C" size_t att_spmm_groups_scratch_bytes(int64_t n_parts, int64_t n_windows) {

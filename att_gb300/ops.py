@@ -199,13 +199,23 @@ def block_convert_finish(pending):
 
 
 def spmm(rowptr, col, val, window_of_part, atomic, X, m_out, window=8, wide=8, out=None,
-         x_scale=None, err_flag=None):
+         x_scale=None, err_flag=None, shape=None):
     """Y[m_out, F] (fp32) = A_blocks X on tensor cores.
 
     X: [n_x, F] fp16 / bf16 (with matching ``val``), fp32 (3xTF32), or
     float8_e4m3fn with ``x_scale`` fp32 [n_x] (values fp16).  F must be a
-    multiple of 8 (16-bit) or 4 (fp32); callers pad otherwise.
+    multiple of 8 (16-bit) or 4 (fp32); callers pad otherwise.  ``shape``: a
+    launch shape returned by ``autotune.tune_spmm`` for this call only (the
+    process-wide defaults otherwise).
     """
+    if shape is not None:
+        from . import autotune
+        autotune.apply_shape(shape)
+        try:
+            return spmm(rowptr, col, val, window_of_part, atomic, X, m_out, window, wide, out,
+                        x_scale, err_flag)
+        finally:
+            autotune.clear_shape()
     require_cuda()
     if X.dim() != 2:
         raise ValueError("X must be 2-D [nodes, features]")

@@ -41,26 +41,19 @@ sys.path.insert(0, ROOT)
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes per launch of the dominant kernel (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum, one launch after two, --clock-control none, GB300),
-# for the workload and scale they were measured on: a profiler counter cannot
-# be read inside the timed run, so the figure is carried here with its source.
+# DRAM bytes per launch of the dominant kernel, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum, --clock-control none, GB300)
+# of the named kernel at the named launch shape on the full-size workload:
+# a profiler counter cannot be read inside the timed run, so the figure is
+# carried here with its source (kernel, shape, the commit it was captured
+# at).  roofline() uses an entry only when the run timed the same launch
+# shape; otherwise it reports traffic null and an algorithmic fraction.
 MEASURED_TRAFFIC = {
     ("spmm_products_fp16", 1.0): {
-        "bytes": 9950022656 + 1406364928, "kernel": "k_spmm16<__half, 8, 64, 8, 3, int>",
-        "ncu_ms": 2.188, "note": "read 9.95 GB + write 1.41 GB; X rows of hub columns hit L2"},
-    ("spmm_products_bf16", 1.0): {
-        "bytes": 9952612096 + 1407312128, "kernel": "k_spmm16<__nv_bfloat16, 8, 64, 8, 2, int, 1>",
-        "ncu_ms": 2.220, "note": "read 9.95 GB + write 1.41 GB; the captured launch was the "
-                                 "autotuner's 2-stage candidate (ring depth does not change "
-                                 "the bytes)"},
-    ("spmm_products_fp8", 1.0): {
-        "bytes": 5507631872 + 1378852096, "kernel": "k_spmm_fp8r<8, 128, 8, int, 1>",
-        "ncu_ms": 2.018, "note": "read 5.51 GB + write 1.38 GB (fp16 kernel: 11.36 GB)"},
-    ("gat_reddit_fp16", 1.0): {
-        "bytes": 591916800 + 229291008, "kernel": "k_gat_fused<__half, 64, 0, 0, int>",
-        "ncu_ms": 2.765, "note": "read 0.59 GB + write 0.23 GB: X' (30 MB) is L2-resident, "
-                                 "the gathers are served by L2"},
+        "bytes": 9950000000 + 1410000000, "shape": ("spmm", 64, 3),
+        "kernel": "k_spmm16<__half, 8, 64, 8, 3, int, 1>", "ncu_ms": 2.14, "commit": "4657d51",
+        "profile": "profiles/spmm16_products_fp16_full_dram.md",
+        "note": "read 9.95 GB + write 1.41 GB; X rows of hub columns hit L2"},
 }
 METRIC = "SpMM/SDDMM HBM GB/s (% roofline); GAT step ms; serve p50/p99 vs plain"
 
@@ -250,6 +243,13 @@ class SpmmProducts(PipelinedE2E):
                           + (self.U * 4 if self.x_kind == "fp8" else 0))
         # the same pass with fp16 features: the yardstick for comparing forms
         self.bytes_fp16 = 4 * (n + 1) + self.nnz * (4 + 2) + self.U * F * 2 + n * F * 4
+        # compulsory: the resident format once, every X row once, Y once (a
+        # lower bound on the DRAM traffic of any schedule)
+        s_v = 2
+        self.bytes_format = (4 * (2 * f.n_parts + 1) + 4 * f.n_condensed
+                             + s_v * f.n_condensed * 8 + 8 * f.n_parts)
+        self.bytes_compulsory = (self.bytes_format + n * F * sx + n * F * 4
+                                 + (n * 4 if self.x_kind == "fp8" else 0))
         self.flops = 2 * self.nnz * F
         self.launches_per_step = 2  # k_zero_uncovered + k_spmm16
         self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz,
@@ -260,17 +260,24 @@ class SpmmProducts(PipelinedE2E):
                        "gathered_rows_U8": self.U, "x_dtype": self.x_kind, "y_dtype": "fp32",
                        "l2": "inputs larger than L2 (no flush)"}
 
+    shape = None  # att_spmm launch shape of every call (None: the library defaults)
+
     def step(self):
         from att_gb300 import ops
         f = self.fmt
         ops.spmm(f.rowptr, f.col, self.val, f.window_of_part, f.atomic, self.Xk, self.n,
-                 out=self.Y, x_scale=self.x_scale)
+                 out=self.Y, x_scale=self.x_scale, shape=self.shape)
 
-    def autotune(self):
-        """Launch shape of att_spmm picked by the autotuner on this graph."""
+    def autotune(self, pinned=None):
+        """Launch shape of att_spmm picked by the autotuner on this graph (or
+        `pinned`, untimed), used by every later call of this workload."""
         from att_gb300 import autotune
+        if pinned is not None:
+            self.shape = tuple(pinned)
+            return {"choice": list(self.shape), "ms_by_shape": None, "pinned": True}
         choice, table = autotune.tune_spmm(self.fmt, self.Xk, self.n, x_scale=self.x_scale,
                                            out=self.Y, val=self.val)
+        self.shape = choice
         return {"choice": list(choice) if choice else None,
                 "ms_by_shape": {"/".join(str(v) for v in k): ms for k, ms in table.items()}}
 
@@ -295,6 +302,20 @@ class SpmmProducts(PipelinedE2E):
     def e2e_step(self):
         self._pipe_step(self._e2e_compute)
 
+    # the plain FP16 drop-in: the reference's own kernel on the fp16 data
+    def plain_available(self):
+        from oracle import ref_spmm
+        return ref_spmm.available() and self.F % 16 == 0
+
+    plain_kind = ("the reference's forward_fp16_gnn kernel (gcn/SpMM/src/spmmKernel.cu:158-265, "
+                  "fp16 accumulation) built for sm_103a, on the fp16 form of the same data")
+
+    def plain_step(self):
+        from oracle import ref_spmm
+        f = self.fmt
+        return ref_spmm.forward_fp16_gnn(f.rowptr, f.col, f.val, f.window_of_part, f.atomic,
+                                         self.X, self.rowptr.shape[0] - 1, self.F, self.n)[0]
+
     def check(self):
         """Size-independent property at full size: A_hat applied to a constant
         column equals the per-row sum of the block values (checksum of checksums)."""
@@ -309,25 +330,31 @@ class SpmmProducts(PipelinedE2E):
         ev = (self.deg[rows].float() * self.deg[self.colidx.long()].float()).half().float()
         rs = torch.zeros(self.rowptr.shape[0] - 1, device=self.X.device).index_add_(0, rows, ev)
         err = ((Y1 - rs[: self.n]).abs().max() / rs.abs().max().clamp_min(1e-30)).item()
-        self.err_vs_fp64 = self.sample_error()
+        from att_gb300 import ops
+        Y = ops.spmm(f.rowptr, f.col, self.val, f.window_of_part, f.atomic, self.Xk, self.n,
+                     x_scale=self.x_scale, shape=self.shape)
+        self.err_vs_fp64 = self.sample_error(Y)
+        if self.x_kind == "fp8":
+            # the kernel's arithmetic alone: FP64 of the dequantized features
+            self.err_vs_fp64_own_inputs = self.sample_error(
+                Y, X64=(self.Xk.float() * self.x_scale[:, None]).double())
+        if self.plain_available():
+            self.plain_err_vs_fp64 = self.sample_error(self.plain_step(), X64=self.X.double())
         return err
 
-    def sample_error(self, rows=20000):
-        """Error of this dtype's kernel against the FP64 product on the
-        unquantized features, for the first `rows` rows of the full graph
-        (normwise max and Frobenius relative)."""
+    def sample_error(self, Y, rows=20000, X64=None):
+        """Error of an output Y against the FP64 product for the first `rows`
+        rows of the full graph (normwise max and Frobenius relative).  X64
+        defaults to the features before this form's rounding (fp16 for the
+        fp16 form, the unquantized fp32 values for bf16 / fp8)."""
         torch = self.torch
-        from att_gb300 import ops
-        import numpy as np
-        f = self.fmt
-        Y = ops.spmm(f.rowptr, f.col, self.val, f.window_of_part, f.atomic, self.Xk, self.n,
-                     x_scale=self.x_scale)
         rows = min(rows, self.n)
         rp = self.rowptr[: rows + 1].long()
         col = self.colidx[: int(rp[-1])].long()
         ridx = torch.repeat_interleave(torch.arange(rows, device=rp.device), rp[1:] - rp[:-1])
         vals = (self.deg[ridx].float() * self.deg[col].float()).half().double()
-        X64 = self.X.double() if self.x_kind == "fp16" else self.Xf64
+        if X64 is None:
+            X64 = self.X.double() if self.x_kind == "fp16" else self.Xf64
         ref = torch.zeros(rows, self.F, dtype=torch.float64, device=rp.device)
         ref.index_add_(0, ridx, vals[:, None] * X64[col])
         got = Y[:rows].double()
@@ -388,6 +415,11 @@ class GatReddit(PipelinedE2E):
         # fused kernel: CSR-granular structure + query rows + gathered rows + output
         self.bytes_fused = 4 * (n + 1) + 4 * self.nnz + n * F * 2 + self.U * F * 2 + n * F * 4
         self.bytes_alg = self.bytes_fused + 2 * n * F * 2  # + the projection's X read, X' write
+        # compulsory for the fused kernel: the resident structure (rowptr pairs,
+        # columns, slot bitmap, window ids) once, X' once, the output once
+        self.bytes_structure = (4 * (2 * f.n_parts + 1) + 4 * f.n_condensed + f.n_condensed
+                                + 4 * f.n_parts)
+        self.bytes_compulsory = self.bytes_structure + n * F * 2 + n * F * 4
         self.flops = 2 * n * F * F + 4 * self.nnz * F
         self.launches_per_step = 2 + (1 if self.G.n_multi else 0)
         self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz, "features": F,
@@ -637,6 +669,7 @@ class GatRedditTF32(GatReddit):
         # the layer's algorithmic bytes with fp32 operands (as the fused count)
         self.bytes_fused = 4 * (n + 1) + 4 * self.nnz + n * F * 4 + self.U * F * 4 + n * F * 4
         self.bytes_alg = self.bytes_fused + 2 * n * F * 4
+        self.bytes_compulsory = self.bytes_structure + n * F * 4 + n * F * 4
         self.config.update({"x_dtype": "fp32 (TF32 tensor cores, 3xTF32 split)",
                             "path": "fused kernel; plain = chain of separate ops"})
 
@@ -684,6 +717,104 @@ class SpmmProductsFP8(SpmmProducts):
     kernel_name = "att_spmm (k_zero_uncovered + k_spmm_fp8r)"
 
 
+class ConvertProducts:
+    """CSR -> row-window block format (8-row windows, 8-wide blocks,
+    partSize 32, fp16 GCN values) of the 2.45M-node graph on the GPU: the
+    reference's blockProcess_fp16_balance (gcn/Block_gcn/example.cpp:48-200)."""
+    name = "convert_products_fp16"
+    unit = "GB/s"
+    e2e_api = "Block_sr_bcrs.blockProcess_fp16_balance (host CSR in, host format out)"
+    kernel_name = ("att_block_plan + att_block_fill (k_unique_*, k_window_counts, scans, "
+                   "k_fill_structure, k_fill_edges)")
+
+    def __init__(self, device, scale=1.0, light=False):
+        import torch
+        from att_gb300 import graphs
+        self.torch = torch
+        c = SpmmProducts
+        n = int(c.N * scale)
+        self.n = n
+        rp, col = graphs.chung_lu(n, c.MEAN_DEG, c.GAMMA, c.SEED, device=device)
+        rp = graphs.pad_rows(rp, 8)
+        deg = graphs.gcn_degree(rp, torch.float16)
+        self.rowptr, self.colidx = rp, col
+        self.deg = torch.where(torch.isfinite(deg), deg, torch.zeros_like(deg))
+        self.nnz = int(col.shape[0])
+        self.config = {"workload": self.name, "nodes": n, "nnz": self.nnz, "gamma": c.GAMMA,
+                       "mean_degree": c.MEAN_DEG, "seed": c.SEED,
+                       "format": "window 8, wide 8, partSize 32, fp16 values"}
+        if light:
+            return
+        self.step()
+        f = self.fmt
+        self.bytes_out = (4 * (2 * f.n_parts + 1) + 4 * f.n_condensed + 2 * f.n_condensed * 8
+                          + 8 * f.n_parts)
+        self.bytes_alg = 4 * (rp.shape[0]) + 4 * self.nnz + 2 * rp.shape[0] + self.bytes_out
+        self.bytes_compulsory = self.bytes_alg
+        self.flops = 0
+        self.launches_per_step = 11
+        self.config.update({"parts": f.n_parts, "condensed_cols": f.n_condensed,
+                            "l2": "inputs and outputs larger than L2 (no flush)"})
+
+    def step(self):
+        from att_gb300 import ops
+        self.fmt = ops.block_convert(self.rowptr, self.colidx, self.deg, window=8, wide=8, part=32)
+
+    def check(self):
+        """Structure of the whole format: rowptr pairs non-decreasing and
+        within the column array, real columns of each part sorted and valid
+        (the full bit-exact comparison with the oracle is a GPU test)."""
+        torch = self.torch
+        f = self.fmt
+        rp = f.rowptr.long()
+        ok = bool((rp[1:] >= rp[:-1]).all()) and int(rp[-1]) == f.n_condensed
+        col = f.col.long()
+        ok = ok and bool(((col >= -1) & (col < self.n)).all())
+        return 0.0 if ok else 1.0
+
+    def e2e_setup(self):
+        torch = self.torch
+        from att_gb300.compat import Block_sr_bcrs
+        self._mod = Block_sr_bcrs
+        self._h = [self.rowptr.cpu().pin_memory(), self.colidx.cpu().pin_memory(),
+                   self.deg.cpu().pin_memory()]
+        self.h2d = sum(t.numel() * t.element_size() for t in self._h)
+        self.d2h = self.bytes_out
+
+    def e2e_step(self):
+        rp, col, deg = self._h
+        self._mod.blockProcess_fp16_balance(rp, col, deg, 8, 8, 32)
+
+    def cpu_port(self):
+        """The oracle's C restatement of the reference's conversion, one host
+        core, the whole graph: (seconds, oracle output)."""
+        from oracle import oracle as orc
+        rp = self.rowptr.cpu().numpy()
+        col = self.colidx.cpu().numpy()
+        deg = self.deg.cpu().numpy()
+        t0 = time.perf_counter()
+        o = orc.block_convert(rp, col, deg, 8, 8, 32)
+        return time.perf_counter() - t0, o
+
+
+def _convert_form(torch, stream, steps, warmup):
+    wl = ConvertProducts("cuda")
+    wl.check()
+    rec = measure(wl, torch, stream, steps, warmup, e2e=False, plain=False)
+    peak, peak_kind = peaks()
+    gbs = wl.bytes_alg / (rec["ms_per_step"] * 1e-3) / 1e9
+    sec, _ = wl.cpu_port()
+    out = {"ms": rec["ms_per_step"], "gbs": gbs, "frac_of_hbm_peak": gbs / peak,
+           "peak_kind": peak_kind, "bytes": wl.bytes_alg,
+           "cpu_baseline": {"value_ms": sec * 1e3, "cores": 1, "kind": "port",
+                            "sample": "the whole graph through oracle/block_oracle.c (the C "
+                                      "restatement of example.cpp:48-200), one host core"},
+           "speedup_vs_cpu": sec * 1e3 / rec["ms_per_step"]}
+    del wl
+    _free(torch)
+    return out
+
+
 class SpmmGcn16k(SpmmProducts):
     """GCN aggregation SpMM on the 16,384-node power-law graph (gamma 2.1,
     mean degree 10, seed 0), X [N, 64] fp16 U[-1,1]: the correctness case of
@@ -704,7 +835,8 @@ class SpmmGcn16k(SpmmProducts):
 WORKLOADS = {SpmmProducts.name: SpmmProducts, GatReddit.name: GatReddit,
              GatRedditTF32.name: GatRedditTF32,
              GatArxivTrain.name: GatArxivTrain, SpmmProductsBF16.name: SpmmProductsBF16,
-             SpmmProductsFP8.name: SpmmProductsFP8, SpmmGcn16k.name: SpmmGcn16k}
+             SpmmProductsFP8.name: SpmmProductsFP8, SpmmGcn16k.name: SpmmGcn16k,
+             ConvertProducts.name: ConvertProducts}
 DEFAULT_WORKLOAD = SpmmProducts.name
 
 
@@ -724,6 +856,12 @@ def cpu_baseline(wl, budget_s=12.0):
     rows = wl.n if wl.n <= 100_000 else max(8, wl.n // 64)
     if isinstance(wl, GatArxivTrain):
         return cpu_baseline_train(wl, threads, budget_s)
+    if isinstance(wl, ConvertProducts):
+        sec, _ = wl.cpu_port()
+        return {"value": wl.bytes_alg / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                "sample": "the whole graph through oracle/block_oracle.c (the C restatement of "
+                          "gcn/Block_gcn/example.cpp:48-200), one host core, one run",
+                "ms_per_sample": sec * 1e3}
     if isinstance(wl, GatReddit):
         rp, col, Xp, rows, b = wl.cpu_sample(rows)
         run = lambda: orc.gat_dot_layer_cpu_fp32(rp, col, Xp)  # noqa: E731
@@ -1081,6 +1219,263 @@ def run_reference_serving(args):
     return 0
 
 
+def _git_head():
+    try:
+        return subprocess.run(["git", "rev-parse", "--short=12", "HEAD"], cwd=ROOT,
+                              stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                              text=True).stdout.strip() or None
+    except Exception:
+        return None
+
+
+def _events(torch, stream, n):
+    return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in range(n)]
+
+
+def _time_each(torch, fn, steps, stream, flush=None):
+    """Per-call device milliseconds of `fn` (CUDA events on `stream`); with
+    `flush`, that buffer is rewritten (L2 flushed) before every call, outside
+    the events."""
+    ev = _events(torch, stream, steps)
+    for a, b in ev:
+        if flush is not None:
+            flush.zero_()
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def roofline(wl, avg_launch_ms, shape):
+    """The dominant kernel's roofline object.
+
+    `frac` is DRAM-based when an ncu capture of the same kernel and launch
+    shape on the same workload exists (MEASURED_TRAFFIC): measured DRAM bytes
+    per launch / the CUDA-event launch time / the measured copy peak.
+    Otherwise it falls back to the algorithmic bytes and says so (those can
+    exceed the peak: they count gathers of hub rows that L2 serves).  Both
+    the algorithmic fraction and the compulsory fraction (format + each X row
+    once + output, a lower bound on DRAM traffic) are always given."""
+    peak, peak_kind = peaks()
+    t = avg_launch_ms * 1e-3
+    kbytes = getattr(wl, "bytes_fused", wl.bytes_alg)
+    alg = kbytes / t / 1e9
+    mt = MEASURED_TRAFFIC.get((wl.name, 1.0 if getattr(wl, "scale", 1.0) == 1.0 else wl.scale))
+    if mt is not None and mt.get("shape") is not None and shape is not None \
+            and tuple(mt["shape"]) != tuple(shape):
+        mt = None  # captured on another launch shape: its bytes are not this kernel's
+    comp = getattr(wl, "bytes_compulsory", None)
+    roof = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
+            "kernel": getattr(wl, "kernel_name", "att_spmm (k_zero_uncovered + k_spmm16)"),
+            "launch_ms": avg_launch_ms, "launch_shape": list(shape) if shape else None,
+            "alg_bytes": kbytes, "alg_achieved": alg, "alg_frac": alg / peak,
+            "compulsory_bytes": comp,
+            "compulsory_frac": (comp / t / 1e9 / peak) if comp else None}
+    if mt is not None:
+        dram = mt["bytes"] / t / 1e9
+        roof.update({"achieved": dram, "frac": dram / peak, "traffic": mt["bytes"],
+                     "basis": "DRAM bytes of one launch of this kernel and shape (ncu) / "
+                              "CUDA-event launch time",
+                     "traffic_source": dict(mt, method="ncu dram__bytes_read.sum + "
+                                                       "dram__bytes_write.sum, one launch")})
+    else:
+        roof.update({"achieved": alg, "frac": alg / peak, "traffic": None,
+                     "basis": "algorithmic bytes / CUDA-event launch time (no DRAM capture "
+                              "of this kernel and shape; can exceed 1 where L2 serves re-reads)"})
+    return roof
+
+
+def measure(wl, torch, stream, steps, warmup, world=1, dist=None, clocks=False, e2e=True,
+            plain=True):
+    """Warm up, time `steps` steps (bracketed by barrier + synchronize), time
+    the dominant kernel per launch, the plain comparison path and the end to
+    end call; returns a dict of the numbers."""
+    from att_gb300 import replicas
+    for _ in range(warmup):
+        wl.step()
+    torch.cuda.synchronize()
+    # workloads whose inputs fit in L2 flush it before every timed step,
+    # outside that step's events (a write of a buffer larger than L2)
+    flush = (torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+             if getattr(wl, "l2_flush", False) else None)
+    sampler = None
+    if clocks:
+        sampler = ClockSampler(torch.cuda.current_device())
+        sampler.start()
+        time.sleep(0.3)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_all0 = torch.cuda.Event(enable_timing=True)
+    t_all1 = torch.cuda.Event(enable_timing=True)
+    t_all0.record(stream)
+    if flush is not None:
+        per_step = _time_each(torch, wl.step, steps, stream, flush)
+    else:
+        for _ in range(steps):
+            wl.step()
+    t_all1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    total_ms = sum(per_step) if flush is not None else t_all0.elapsed_time(t_all1)
+    # dominant kernel alone, per launch, for the roofline
+    kernel_step = getattr(wl, "kernel_step", wl.step)
+    if hasattr(wl, "prepare_kernel"):
+        wl.prepare_kernel()
+    torch.cuda.synchronize()
+    per_launch = sorted(_time_each(torch, kernel_step, steps, stream, flush))
+    clk = sampler.stop() if sampler else None
+    total_ms = replicas.max_over_ranks([total_ms], device="cuda")[0] if world > 1 else total_ms
+    rec = {"ms_per_step": total_ms / steps, "per_launch": per_launch,
+           "avg_launch_ms": sum(per_launch) / len(per_launch), "clocks": clk}
+    # the plain comparison path on the same data
+    rec["plain_ms"] = None
+    if plain and getattr(wl, "plain_step", None) and getattr(wl, "plain_available", lambda: True)():
+        for _ in range(2):
+            wl.plain_step()
+        torch.cuda.synchronize()
+        n_plain = max(3, min(steps, 10))
+        pt = _time_each(torch, wl.plain_step, n_plain, stream, flush)
+        rec["plain_ms"] = sum(pt) / len(pt)
+    # end to end through the reference-facing call with host buffers
+    if e2e:
+        wl.e2e_setup()
+        # freshly pinned host buffers move slowly on their first passes (the
+        # first e2e pass of a process measured 16.7 ms against 7.4 ms once
+        # warm), so every buffer set is cycled several times first
+        for _ in range(10):
+            wl.e2e_step()
+        torch.cuda.synchronize()
+        e_steps = max(3, min(steps, 20))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        if hasattr(wl, "e2e_begin"):
+            wl.e2e_begin()
+        for _ in range(e_steps):
+            wl.e2e_step()
+        if hasattr(wl, "e2e_finish"):
+            wl.e2e_finish()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1) / e_steps
+        rec["e2e_ms"] = replicas.max_over_ranks([e2e_ms], device="cuda")[0] if world > 1 else e2e_ms
+    return rec
+
+
+def _free(torch):
+    import gc
+    gc.collect()
+    torch.cuda.empty_cache()
+
+
+def _spmm_form(cls, torch, stream, steps, warmup):
+    wl = cls("cuda")
+    tuned = wl.autotune()
+    wl.check()
+    rec = measure(wl, torch, stream, steps, warmup, e2e=False)
+    out = {"ms": rec["ms_per_step"], "kernel_launch_ms": rec["avg_launch_ms"],
+           "gbs_own_bytes": wl.bytes_alg / (rec["ms_per_step"] * 1e-3) / 1e9,
+           "gbs_fp16_equivalent": wl.bytes_fp16 / (rec["ms_per_step"] * 1e-3) / 1e9,
+           "err_vs_fp64": wl.err_vs_fp64,
+           "plain_fp16_dropin_ms": rec["plain_ms"],
+           "plain": wl.plain_kind if rec["plain_ms"] is not None else None,
+           "speedup_vs_plain": (rec["plain_ms"] / rec["ms_per_step"]) if rec["plain_ms"] else None,
+           "launch_shape": tuned["choice"] if tuned else None}
+    if hasattr(wl, "err_vs_fp64_own_inputs"):
+        out["err_vs_fp64_of_dequantized_inputs"] = wl.err_vs_fp64_own_inputs
+    del wl
+    _free(torch)
+    return out
+
+
+def _gat_form(cls, torch, stream, steps, warmup):
+    wl = cls("cuda")
+    wl.check()
+    rec = measure(wl, torch, stream, steps, warmup, e2e=False)
+    out = {"ms": rec["ms_per_step"], "fused_launch_ms": rec["avg_launch_ms"],
+           "alg_gbs": wl.bytes_alg / (rec["ms_per_step"] * 1e-3) / 1e9,
+           "err_vs_fp64": wl.err_vs_fp64,
+           "plain_chain_ms": rec["plain_ms"],
+           "plain": "the reference's chain of separate ops (SDDMM, edge softmax, SpMM of edge "
+                    "values; end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198) on this "
+                    "package's drop-in kernels (the reference's GAT kernels ship no source)",
+           "speedup_vs_plain": (rec["plain_ms"] / rec["ms_per_step"]) if rec["plain_ms"] else None}
+    if hasattr(wl, "chain_err_vs_fp64"):
+        out["plain_chain_err_vs_fp64"] = wl.chain_err_vs_fp64
+    del wl
+    _free(torch)
+    return out
+
+
+def _train_form(torch, stream, steps, warmup):
+    wl = GatArxivTrain("cuda")
+    grad_diff = wl.check()
+    rec = measure(wl, torch, stream, steps, warmup, e2e=False)
+    out = {"ms": rec["ms_per_step"], "plain_chain_ms": rec["plain_ms"],
+           "plain": "the same 2-layer GAT on the reference's chain of separate ops (fp16 "
+                    "drop-ins, torch autograd glue), same GPU",
+           "speedup_vs_plain": (rec["plain_ms"] / rec["ms_per_step"]) if rec["plain_ms"] else None,
+           "layer1_weight_grad_rel_diff_fused_vs_chain": grad_diff}
+    del wl
+    _free(torch)
+    return out
+
+
+def _serve_form(torch, requests=200, seeds=(4, 5, 6)):
+    """p50 / p99 of the continuous-batching server and of one graph per call
+    on Poisson traces of `requests` requests per seed (200 req/s)."""
+    from att_gb300 import serving
+    pool, model = _serve_pool_and_model(1.0)
+    srv = serving.Server(model, budget=120e9, max_active=64, workers=2, keep_outputs=False)
+    srv.run(serving.make_requests(pool, SERVE_RATE, 100, SERVE_SEED + 100), realtime=True)
+    serving.serve_one_by_one(serving.make_requests(pool, SERVE_RATE, 50, SERVE_SEED + 101),
+                             model, realtime=True, keep_outputs=False)
+    out = {"requests_per_seed": requests, "rate_per_s": SERVE_RATE, "seeds": list(seeds),
+           "p50_ms": [], "p99_ms": [], "plain_p50_ms": [], "plain_p99_ms": []}
+    for sd in seeds:
+        reqs = serving.make_requests(pool, SERVE_RATE, requests, sd)
+        srv.run(reqs, realtime=True)
+        st = serving.latency_stats(reqs)
+        plain = [serving.Request(r.rid, r.arrival, r.rowptr, r.col, r.X, r.n, r.nnz) for r in reqs]
+        serving.serve_one_by_one(plain, model, realtime=True, keep_outputs=False)
+        pst = serving.latency_stats(plain)
+        out["p50_ms"].append(st["p50_ms"])
+        out["p99_ms"].append(st["p99_ms"])
+        out["plain_p50_ms"].append(pst["p50_ms"])
+        out["plain_p99_ms"].append(pst["p99_ms"])
+    del pool, srv
+    _free(torch)
+    return out
+
+
+def run_forms(torch, stream, steps, warmup, skip=()):
+    """The benchmark spec's chosen forms beside their plain paths, each measured
+    on its own workload after the headline one (a few seconds each)."""
+    forms = {}
+    jobs = [("spmm_products_bf16", lambda: _spmm_form(SpmmProductsBF16, torch, stream, steps, warmup)),
+            ("spmm_products_fp8", lambda: _spmm_form(SpmmProductsFP8, torch, stream, steps, warmup)),
+            ("gat_reddit_fp16", lambda: _gat_form(GatReddit, torch, stream, steps, warmup)),
+            ("gat_reddit_tf32", lambda: _gat_form(GatRedditTF32, torch, stream, steps, warmup)),
+            ("gat_arxiv_train_bf16", lambda: _train_form(torch, stream, steps, warmup)),
+            ("convert_products_fp16", lambda: _convert_form(torch, stream, steps, warmup)),
+            ("spmm_gcn16k_fp16", lambda: _spmm_form(SpmmGcn16k, torch, stream, steps, warmup)),
+            ("serve_gcn_fp16", lambda: _serve_form(torch))]
+    for name, fn in jobs:
+        if name in skip:
+            continue
+        t0 = time.time()
+        try:
+            forms[name] = fn()
+        except Exception as exc:  # one form failing must not hide the others
+            forms[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+        forms[name]["wall_s"] = time.time() - t0
+    return forms
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1089,8 +1484,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVE])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the other forms (measured after the headline workload)")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="node-count scale of the workload (1.0 = the named config)")
+    ap.add_argument("--shape", default=None,
+                    help="pin the SpMM launch shape instead of autotuning it, e.g. spmm,64,3 "
+                         "(for profiler captures of a known kernel)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload == SERVE:
@@ -1113,118 +1513,28 @@ def main():
     _lib.load()
 
     wl = WORKLOADS[args.workload]("cuda", scale=args.scale)
-    tuned = wl.autotune() if hasattr(wl, "autotune") else None
+    wl.scale = args.scale
+    pinned = None
+    if args.shape:
+        pinned = tuple(int(v) if v.isdigit() else v for v in args.shape.split(","))
+    tuned = wl.autotune(pinned) if hasattr(wl, "autotune") else None
     check_err = wl.check()
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        wl.step()
-    torch.cuda.synchronize()
-
-    # workloads whose inputs fit in L2 flush it before every timed step,
-    # outside that step's events (a write of a buffer larger than L2)
-    flush = (torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-             if getattr(wl, "l2_flush", False) else None)
-
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t_all0 = torch.cuda.Event(enable_timing=True)
-    t_all1 = torch.cuda.Event(enable_timing=True)
-    t_all0.record(stream)
-    step_ev = []
-    for k in range(args.steps):
-        if flush is not None:
-            flush.zero_()
-            step_ev.append((torch.cuda.Event(enable_timing=True),
-                            torch.cuda.Event(enable_timing=True)))
-            step_ev[-1][0].record(stream)
-        wl.step()
-        if flush is not None:
-            step_ev[-1][1].record(stream)
-    t_all1.record(stream)
-    torch.cuda.synchronize()
-    # dominant kernel alone, per launch, for the roofline
-    kernel_step = getattr(wl, "kernel_step", wl.step)
-    if hasattr(wl, "prepare_kernel"):
-        wl.prepare_kernel()
-    torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    for k in range(args.steps):
-        if flush is not None:
-            flush.zero_()
-        ev[k][0].record(stream)
-        kernel_step()
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    clocks = sampler.stop()
-    total_ms = (sum(a.elapsed_time(b) for a, b in step_ev) if flush is not None
-                else t_all0.elapsed_time(t_all1))
-    per_launch = sorted(a.elapsed_time(b) for a, b in ev)
-    avg_launch_ms = sum(per_launch) / len(per_launch)
-    from att_gb300 import replicas
-    total_ms = replicas.max_over_ranks([total_ms], device="cuda")[0]
-    ms_per_step = total_ms / args.steps
+    rec = measure(wl, torch, stream, args.steps, args.warmup, world=world, dist=dist,
+                  clocks=True)
+    ms_per_step = rec["ms_per_step"]
     is_time = wl.unit == "ms"
+    from att_gb300 import replicas
     value = (ms_per_step if is_time
              else replicas.aggregate_rate(wl.bytes_alg, ms_per_step, world) / 1e9)
-    plain_ms = None
-    if getattr(wl, "plain_step", None):
-        for _ in range(2):
-            wl.plain_step()
-        torch.cuda.synchronize()
-        p0 = torch.cuda.Event(enable_timing=True)
-        p1 = torch.cuda.Event(enable_timing=True)
-        p0.record(stream)
-        for _ in range(max(3, min(args.steps, 10))):
-            wl.plain_step()
-        p1.record(stream)
-        torch.cuda.synchronize()
-        plain_ms = p0.elapsed_time(p1) / max(3, min(args.steps, 10))
-
-    # end to end through the drop-in with host buffers
-    wl.e2e_setup()
-    for _ in range(2):
-        wl.e2e_step()
-    torch.cuda.synchronize()
-    e_steps = max(3, min(args.steps, 20))
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    if hasattr(wl, "e2e_begin"):
-        wl.e2e_begin()
-    for _ in range(e_steps):
-        wl.e2e_step()
-    if hasattr(wl, "e2e_finish"):
-        wl.e2e_finish()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e_steps
-    e2e_ms = replicas.max_over_ranks([e2e_ms], device="cuda")[0]
-
-    peak, peak_kind = peaks()
-    kbytes = getattr(wl, "bytes_fused", wl.bytes_alg)
-    achieved = kbytes / (avg_launch_ms * 1e-3) / 1e9
+    e2e_ms = rec["e2e_ms"]
+    shape = tuple(tuned["choice"]) if tuned and tuned.get("choice") else None
     line = None
     if rank == 0:
         base = None
         if not args.no_cpu_baseline:
             base = cpu_baseline(wl)
-        mt = MEASURED_TRAFFIC.get((wl.name, args.scale))
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": mt["bytes"] if mt else None,
-                "traffic_source": (dict(mt, method="ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                                   "one launch") if mt else None),
-                "dram_gbs_at_bench_time": (mt["bytes"] / (avg_launch_ms * 1e-3) / 1e9) if mt else None,
-                "peak_kind": peak_kind,
-                "kernel": getattr(wl, "kernel_name", "att_spmm (k_zero_uncovered + k_spmm16)")
-                          + ", avg of %d launches" % args.steps,
-                "bytes_per_launch": kbytes}
+        per_launch = rec["per_launch"]
         line = {"metric": METRIC, "value": value, "unit": wl.unit, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
                 "higher_is_better": not is_time, "scaling": "weak", "vs_baseline": None,
@@ -1233,7 +1543,7 @@ def main():
                 "data": "synthetic",
                 "config": dict(wl.config),
                 "workload_ms_per_step": ms_per_step,
-                "roofline": roof,
+                "roofline": roofline(wl, rec["avg_launch_ms"], shape),
                 "cpu_baseline": ({k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
                                  if base else None),
                 "e2e": {"value": e2e_ms if is_time else world * wl.bytes_alg / (e2e_ms * 1e-3) / 1e9,
@@ -1241,15 +1551,26 @@ def main():
                         "h2d_bytes_per_step": wl.h2d, "d2h_bytes_per_step": wl.d2h,
                         "ms_per_step": e2e_ms, "api": wl.e2e_api},
                 "gpu_launches": wl.launches_per_step * args.steps,
-                "clocks": clocks,
+                "clocks": rec["clocks"],
                 "gflops": world * wl.flops / (ms_per_step * 1e-3) / 1e9,
-                "plain_dropin_ms_per_step": plain_ms,
+                "plain_dropin_ms_per_step": rec["plain_ms"],
+                "plain_dropin": getattr(wl, "plain_kind", None) if rec["plain_ms"] else None,
+                "speedup_vs_plain_dropin": (rec["plain_ms"] / ms_per_step) if rec["plain_ms"] else None,
                 "autotune": tuned,
                 "fp16_equivalent_gbs": (world * wl.bytes_fp16 / (ms_per_step * 1e-3) / 1e9
                                         if hasattr(wl, "bytes_fp16") else None),
                 "check_rel_err": check_err,
                 "err_vs_fp64": getattr(wl, "err_vs_fp64", None),
-                "launch_ms_p50": per_launch[len(per_launch) // 2]}
+                "plain_dropin_err_vs_fp64": getattr(wl, "plain_err_vs_fp64", None),
+                "launch_ms_p50": per_launch[len(per_launch) // 2],
+                "commit": _git_head()}
+        if hasattr(wl, "err_vs_fp64_own_inputs"):
+            line["err_vs_fp64_of_dequantized_inputs"] = wl.err_vs_fp64_own_inputs
+    if rank == 0 and world == 1 and not args.no_forms:
+        del wl
+        _free(torch)
+        line["forms"] = run_forms(torch, stream, min(args.steps, 10), 3, skip=(args.workload,))
+    if rank == 0:
         print(json.dumps(line))
     if world > 1:
         dist.barrier()

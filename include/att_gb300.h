@@ -60,7 +60,12 @@ enum att_dtype {
     ATT_NONE = -1
 };
 
-/* Process-wide tuning knobs (no counterpart in the reference).
+/* Tuning knobs (no counterpart in the reference).  att_set_option sets the
+ * process-wide default of a knob; att_set_thread_option overrides it for the
+ * calling host thread only (-1 returns the thread to the default), so a
+ * caller can fix the launch shape of its own calls without changing other
+ * threads' calls; att_get_option reads the value in effect on the calling
+ * thread.
  *   "spmm_gather": 0 = 16-byte cp.async row gathers (default),
  *                  1 = TMA tile::gather4 row gathers (F >= 64),
  *                  2 = one cp.async.bulk per gathered row (8-row windows,
@@ -72,6 +77,7 @@ enum att_dtype {
  *   "spmm_tf32":   fp32-feature (3xTF32) kernel, features per item x ring
  *                  depth: 0 = 64 x 4 (default), 1 = 32 x 3, 2 = 32 x 4, 3 = 64 x 2. */
 ATT_API int att_set_option(const char *key, int value);
+ATT_API int att_set_thread_option(const char *key, int value);
 ATT_API int att_get_option(const char *key, int *value);
 
 /* Human-readable name of a status. */

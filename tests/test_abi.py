@@ -64,3 +64,40 @@ def test_ops_refuse_without_cuda():
     from att_gb300 import ops
     with pytest.raises(RuntimeError):
         ops.require_cuda()
+
+
+def test_thread_option_overrides_only_the_calling_thread(lib):
+    """att_set_thread_option changes the launch shape of the calling thread's
+    calls only; -1 returns it to the process-wide default."""
+    import threading
+    from att_gb300 import autotune
+    v = ctypes.c_int()
+    assert lib.att_get_option(b"spmm_stages", ctypes.byref(v)) == 0
+    default = v.value
+    other = 2 if default != 2 else 4
+    seen = {}
+
+    def worker():
+        assert lib.att_set_thread_option(b"spmm_stages", other) == 0
+        w = ctypes.c_int()
+        lib.att_get_option(b"spmm_stages", ctypes.byref(w))
+        seen["worker"] = w.value
+        seen["main_during"] = None
+        ev_set.set()
+        ev_done.wait(5)
+
+    ev_set, ev_done = threading.Event(), threading.Event()
+    t = threading.Thread(target=worker)
+    t.start()
+    ev_set.wait(5)
+    lib.att_get_option(b"spmm_stages", ctypes.byref(v))
+    assert v.value == default and seen["worker"] == other
+    ev_done.set()
+    t.join()
+    autotune.apply_shape(("spmm", 128, other))
+    lib.att_get_option(b"spmm_fc", ctypes.byref(v))
+    assert v.value == 128
+    autotune.clear_shape()
+    lib.att_get_option(b"spmm_stages", ctypes.byref(v))
+    assert v.value == default
+    assert lib.att_set_thread_option(b"spmm_stages", 7) == 1  # invalid value refused

@@ -303,9 +303,10 @@ def restore_spmm_options():
 
 @pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16, torch.float8_e4m3fn,
                                    torch.float32])
-def test_autotune_spmm_sets_a_measured_shape(cuda, restore_spmm_options, dtype):
-    """tune_spmm times every candidate shape, leaves the fastest set (read
-    back through att_get_option) and the tuned launch gives the default
+def test_autotune_spmm_picks_a_measured_shape(cuda, restore_spmm_options, dtype):
+    """tune_spmm times every candidate shape and returns the fastest without
+    changing the options in effect afterwards (read back through
+    att_get_option); the chosen shape, passed per call, gives the default
     shape's result (same arithmetic; atomics may reorder fp32 adds)."""
     from att_gb300 import _lib, autotune, graphs, ops
     import ctypes
@@ -321,23 +322,24 @@ def test_autotune_spmm_sets_a_measured_shape(cuda, restore_spmm_options, dtype):
     else:
         Xk = X.to(dtype).cuda()
         val = f.val.to(dtype)
+
+    def options():
+        got = {}
+        for k in (b"spmm_fc", b"spmm_stages", b"spmm_fp8", b"spmm_tf32"):
+            v = ctypes.c_int(0)
+            _lib.call("att_get_option", k, ctypes.byref(v))
+            got[k] = v.value
+        return got
+    before = options()
     Y0 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale)
     tuner = autotune.Tuner(warmup=1, reps=3)
     choice, table = autotune.tune_spmm(f, Xk, 2000, x_scale=scale, val=val, tuner=tuner)
     assert set(table) == set(autotune.spmm_candidates(dtype, 128))
     assert choice == min(table, key=table.get)
-    got = {}
-    for k in (b"spmm_fc", b"spmm_stages", b"spmm_fp8", b"spmm_tf32"):
-        v = ctypes.c_int(0)
-        _lib.call("att_get_option", k, ctypes.byref(v))
-        got[k] = v.value
-    if choice[0] == "spmm":
-        assert (got[b"spmm_fc"], got[b"spmm_stages"]) == choice[1:]
-    elif choice[0] == "tf32":
-        assert got[b"spmm_tf32"] == choice[1]
-    else:
-        assert got[b"spmm_fp8"] == choice[1]
-    Y1 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale)
+    assert options() == before
+    Y1 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale,
+                  shape=choice)
+    assert options() == before
     assert oracle.rel_err(Y1.cpu().numpy(), Y0.cpu().numpy()) <= 1e-6
 
 
