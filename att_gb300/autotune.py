@@ -72,18 +72,12 @@ class Tuner:
 _default = Tuner()
 
 
-def _set(key, value):
-    """Override a launch-shape knob for the calling thread only."""
-    _lib.call("att_set_thread_option", key.encode(), int(value))
-
-
 SHAPE_KNOBS = ("spmm_fc", "spmm_stages", "spmm_fp8", "spmm_tf32")
 
 
 def clear_shape():
     """Return the calling thread to the process-wide launch-shape defaults."""
-    for k in SHAPE_KNOBS:
-        _set(k, -1)
+    ops.set_launch_shape(None)
 
 
 def spmm_candidates(x_dtype, F):
@@ -100,15 +94,7 @@ def spmm_candidates(x_dtype, F):
 
 def apply_shape(c):
     """Set the calling thread's att_spmm launch shape to candidate `c`."""
-    if c is None:
-        return
-    if c[0] == "spmm":
-        _set("spmm_fc", c[1])
-        _set("spmm_stages", c[2])
-    elif c[0] == "fp8":
-        _set("spmm_fp8", c[1])
-    elif c[0] == "tf32":
-        _set("spmm_tf32", c[1])
+    ops.set_launch_shape(c)
 
 
 def tune_spmm(fmt, X, m_out, x_scale=None, out=None, val=None, tuner=None):
@@ -129,11 +115,16 @@ def tune_spmm(fmt, X, m_out, x_scale=None, out=None, val=None, tuner=None):
 
     vals = fmt.val if val is None else val
 
+    cur = [None]
+
+    def setup(c):
+        cur[0] = c
+
     def run():
         ops.spmm(fmt.rowptr, fmt.col, vals, fmt.window_of_part, fmt.atomic, X, m_out,
-                 window=fmt.window, wide=fmt.wide, out=Y, x_scale=x_scale)
+                 window=fmt.window, wide=fmt.wide, out=Y, x_scale=x_scale, shape=cur[0])
     try:
-        return tuner.best(key, cands, apply_shape, run)
+        return tuner.best(key, cands, setup, run)
     finally:
         clear_shape()
 

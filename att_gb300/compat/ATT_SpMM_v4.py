@@ -34,14 +34,25 @@ def spmm_fp16_m_h2(row_pointers, column_index, degrees, vals, window, automic, X
     return [Y.reshape(M, -1)]
 
 
+def _col(v):
+    """Per-head vectors of node values as [h, M, 1] (accepts [h, M, 1] or
+    [h, 1, M]: the caller's comments describe the latter, this package's row
+    sums return the former)."""
+    return v if v.shape[-1] == 1 else v.transpose(1, 2)
+
+
 def bmm_v_m(a0_tmp, a1_tmp, X):
-    """a*_tmp [h, M, 1], X [h, F, M] -> ([h, 1, F], [h, 1, F])."""
-    g0 = torch.bmm(X, a0_tmp.to(X.dtype)).transpose(1, 2)
-    g1 = torch.bmm(X, a1_tmp.to(X.dtype)).transpose(1, 2)
+    """Attention-vector gradients (mgat_conv.py:82): a*_grad[h, 0, f] =
+    sum_m a*_tmp[h, m] X[h, f, m]; a*_tmp [h, M, 1] (or [h, 1, M]), X
+    [h, F, M] -> ([h, 1, F], [h, 1, F])."""
+    g0 = torch.bmm(X, _col(a0_tmp).to(X.dtype)).transpose(1, 2)
+    g1 = torch.bmm(X, _col(a1_tmp).to(X.dtype)).transpose(1, 2)
     return g0, g1
 
 
 def bmm_v_v(temp_grad, temp_a):
-    """temp_grad [h, M, 1], temp_a [h, 1, F] -> [M, h*F] (outer products per head)."""
-    out = torch.bmm(temp_grad.to(temp_a.dtype), temp_a)  # [h, M, F]
+    """Feature gradient (mgat_conv.py:94): out[m, h*F + f] = temp_grad[h, m] *
+    temp_a[h, 0, f]; temp_grad [h, M, 1] (or [h, 1, M]), temp_a [h, 1, F] ->
+    [M, h*F]."""
+    out = torch.bmm(_col(temp_grad).to(temp_a.dtype), temp_a)  # [h, M, F]
     return [out.permute(1, 0, 2).reshape(out.shape[1], -1)]

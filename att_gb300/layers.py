@@ -12,6 +12,8 @@ fused kernels.
 * ``MGATFunction_multi``, ``MGATSpmm_multi``, ``MGATSpmm1_multi``,
   ``GATConv_multi`` -- end2end_head/gat_final/mgat_csr/mgat_conv.py:14-198
   (the multi-head v3 chain of separate ops: the "plain" drop-in path).
+* ``MGATv2Function_multi``, ``GATv2Conv_multi`` --
+  end2end_head/gatv2_final/mgat_csr/mgat_conv.py:14-196 (GATv2 on the same ops).
 * ``GATNet`` -- the reference's Net (end2end_ori/gat_final/mgat_csr/gat_mgnn.py:17-40)
   with either that chain or the fused kernels (att_gb300.gat.GATConv).
 """
@@ -262,6 +264,75 @@ class GATConv_multi(nn.Module):
         rows_sum = MGATSpmm1_multi.apply(att, inputInfo)
         att = self.dropout(att)
         h_prime = MGATSpmm_multi.apply(att, X_prime, inputInfo)
+        return h_prime.div(rows_sum)  # [M, h, F]
+
+
+# ---------------------------------------------------------------------------
+# GATv2, multi-head (end2end_head/gatv2_final/mgat_csr/mgat_conv.py:14-196)
+# ---------------------------------------------------------------------------
+class MGATv2Function_multi(torch.autograd.Function):
+    """att[h][e(i,j)] = X0'[h][i].a[h] + X1'[h][j].a[h] (attv2_fp16_h_nnz,
+    mgat_conv.py:14-31) with its backward (mgat_conv.py:33-66): the row sums
+    of the incoming gradient pair with X0' and the column sums (mirrored map)
+    with X1'."""
+
+    @staticmethod
+    def forward(ctx, X_prime0, X_prime1, a0, inputInfo):
+        ctx.inputInfo = inputInfo
+        ctx.save_for_backward(X_prime0, X_prime1, a0)
+        return ATT_SDDMM_v3.attv2_fp16_h_nnz(inputInfo.row_pointers, inputInfo.column_index,
+                                             inputInfo.degrees, inputInfo.window, X_prime0,
+                                             X_prime1, a0, inputInfo.max,
+                                             inputInfo.num_edges)[0]
+
+    @staticmethod
+    def backward(ctx, att_grad):
+        X_prime0, X_prime1, a0 = ctx.saved_tensors
+        inputInfo = ctx.inputInfo
+        att_grad = att_grad.contiguous()
+        col_sum = ATT_SpMM_v3.spmm_fp16_h_m_rowsum(
+            inputInfo.row_pointers, inputInfo.degrees_trans, att_grad, inputInfo.window,
+            inputInfo.automic, inputInfo.num_nodes_ori)[0].half()
+        row_sum = ATT_SpMM_v3.spmm_fp16_h_m_rowsum(
+            inputInfo.row_pointers, inputInfo.degrees, att_grad, inputInfo.window,
+            inputInfo.automic, inputInfo.num_nodes_ori)[0].half()
+        a_grad = (torch.bmm(row_sum.transpose(1, 2), X_prime0)
+                  + torch.bmm(col_sum.transpose(1, 2), X_prime1))
+        return torch.bmm(row_sum, a0), torch.bmm(col_sum, a0), a_grad, None
+
+
+class GATv2Conv_multi(nn.Module):
+    """The reference's multi-head GATv2 layer over the separate drop-in ops
+    (fp16; mgat_conv.py:151-196): two projections, each through LeakyReLU;
+    attv2 logits; per-head min-max scaling over all edges; exp; row sums;
+    SpMM of the edge values with X1'; divide."""
+
+    def __init__(self, input_dim, output_dim, dropout, alpha, head):
+        super().__init__()
+        gain = nn.init.calculate_gain("relu")
+        self.fc0 = nn.Linear(input_dim, output_dim * head, bias=False)
+        nn.init.xavier_normal_(self.fc0.weight.data, gain=gain)
+        self.fc1 = nn.Linear(input_dim, output_dim * head, bias=False)
+        nn.init.xavier_normal_(self.fc1.weight.data, gain=gain)
+        self.a0 = nn.Parameter(torch.zeros(head, 1, output_dim))
+        nn.init.xavier_normal_(self.a0.data, gain=gain)
+        self.output_dim, self.head = output_dim, head
+        self.dropout = nn.Dropout(dropout)
+        self.leakyrelu = nn.LeakyReLU(alpha)
+
+    def forward(self, X, inputInfo):
+        H, Fo = self.head, self.output_dim
+        X_prime0 = F.linear(X.half(), self.fc0.weight.half())
+        X_prime1 = F.linear(X.half(), self.fc1.weight.half())
+        X_prime0 = self.leakyrelu(X_prime0.view(-1, H, Fo).permute(1, 0, 2).contiguous())
+        X_prime1 = self.leakyrelu(X_prime1.view(-1, H, Fo).permute(1, 0, 2).contiguous())
+        att = MGATv2Function_multi.apply(X_prime0, X_prime1, self.a0.half(), inputInfo)
+        max_value = torch.max(att, dim=1, keepdim=True)[0]
+        min_value = torch.min(att, dim=1, keepdim=True)[0]
+        att = torch.exp((att - min_value) / (max_value - min_value))
+        rows_sum = MGATSpmm1_multi.apply(att, inputInfo)
+        att = self.dropout(att)
+        h_prime = MGATSpmm_multi.apply(att, X_prime1, inputInfo)
         return h_prime.div(rows_sum)  # [M, h, F]
 
 

@@ -4,6 +4,7 @@ Tensors live on the current CUDA device; every kernel launches on
 ``torch.cuda.current_stream()``.  Outputs and workspaces are allocated with
 torch (the caching allocator) and handed to the C ABI as raw pointers.
 """
+import threading
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -198,6 +199,28 @@ def block_convert_finish(pending):
                       *pending.options)
 
 
+_SHAPE_KNOBS = {"spmm": ("spmm_fc", "spmm_stages"), "fp8": ("spmm_fp8",),
+                "tf32": ("spmm_tf32",)}
+_ALL_KNOBS = ("spmm_fc", "spmm_stages", "spmm_fp8", "spmm_tf32")
+_tls = threading.local()
+
+
+def set_launch_shape(shape):
+    """Make the calling thread's att_spmm launch shape `shape` (an autotuner
+    candidate such as ("spmm", 64, 3); None = the process-wide defaults).  The
+    thread's current shape is remembered, so repeating it costs no call into
+    the library."""
+    cur = getattr(_tls, "shape", None)
+    if cur == shape:
+        return
+    for k in _ALL_KNOBS:
+        _lib.call("att_set_thread_option", k.encode(), -1)
+    if shape is not None:
+        for k, v in zip(_SHAPE_KNOBS[shape[0]], shape[1:]):
+            _lib.call("att_set_thread_option", k.encode(), int(v))
+    _tls.shape = None if shape is None else tuple(shape)
+
+
 def spmm(rowptr, col, val, window_of_part, atomic, X, m_out, window=8, wide=8, out=None,
          x_scale=None, err_flag=None, shape=None):
     """Y[m_out, F] (fp32) = A_blocks X on tensor cores.
@@ -205,17 +228,10 @@ def spmm(rowptr, col, val, window_of_part, atomic, X, m_out, window=8, wide=8, o
     X: [n_x, F] fp16 / bf16 (with matching ``val``), fp32 (3xTF32), or
     float8_e4m3fn with ``x_scale`` fp32 [n_x] (values fp16).  F must be a
     multiple of 8 (16-bit) or 4 (fp32); callers pad otherwise.  ``shape``: a
-    launch shape returned by ``autotune.tune_spmm`` for this call only (the
-    process-wide defaults otherwise).
+    launch shape returned by ``autotune.tune_spmm`` (the process-wide
+    defaults when None).
     """
-    if shape is not None:
-        from . import autotune
-        autotune.apply_shape(shape)
-        try:
-            return spmm(rowptr, col, val, window_of_part, atomic, X, m_out, window, wide, out,
-                        x_scale, err_flag)
-        finally:
-            autotune.clear_shape()
+    set_launch_shape(shape)
     require_cuda()
     if X.dim() != 2:
         raise ValueError("X must be 2-D [nodes, features]")

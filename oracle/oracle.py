@@ -27,6 +27,10 @@ Contents
                                   benchmark-v3/spmm-benchmark/test/spmm_fp16/test_spmm_h_m.py:45-66,
                                   test_spmm_h_m_ones.py:45-68
   - GAT layer forward (v1 chain)  end2end_ori/gat_final/mgat_csr/mgat_conv.py:173-198
+  - GATv2 layer (differentiable)  end2end_head/gatv2_final/mgat_csr/mgat_conv.py:151-196
+* Row-sampled FP64 restatements for full-size graphs (sub_csr, sample_rows,
+  spmm_rows_fp64, gat_dot_rows_fp64, gat_add_rows_torch) and the 2-layer GCN
+  of the serving loop (gcn2_fp64).
 """
 import ctypes
 import os
@@ -370,6 +374,34 @@ def gat_add_layer_torch(rowptr, col, Xp, a0, a1, slope=0.2):
     p = ex / l[rows]
     out = torch.zeros(N, H, F, dtype=e.dtype).index_add(0, rows, p[:, :, None] * X3[col])
     return out.reshape(N, H * F)
+
+
+def gatv2_layer_torch(rowptr, col, X, W0, W1, a, slope=0.2, n_out=None):
+    """Differentiable torch restatement (use fp64 tensors) of the reference's
+    GATv2 layer (end2end_head/gatv2_final/mgat_csr/mgat_conv.py:151-196, no
+    dropout): X0' = LeakyReLU(X W0), X1' = LeakyReLU(X W1) per head;
+    e_ij = X0'_i.a + X1'_j.a; per head e is scaled to [0, 1] by its minimum
+    and maximum over all edges; p = exp(e) / row sum; out_i = sum_j p_ij X1'_j.
+    X [N, D], W0 / W1 [D, H*F], a [H, 1, F] -> [N, H, F]."""
+    import torch
+    rowptr = torch.as_tensor(rowptr).long()
+    col = torch.as_tensor(col).long()
+    H, _, Fo = a.shape
+    N = rowptr.numel() - 1
+    lr = torch.nn.functional.leaky_relu
+    X0 = lr((X @ W0).view(-1, H, Fo), slope)
+    X1 = lr((X @ W1).view(-1, H, Fo), slope)
+    rows = torch.repeat_interleave(torch.arange(N), rowptr[1:] - rowptr[:-1])
+    s0 = (X0 * a[:, 0][None]).sum(-1)  # [N, H]
+    s1 = (X1 * a[:, 0][None]).sum(-1)
+    e = s0[rows] + s1[col]              # [nnz, H]
+    mn = e.min(0, keepdim=True).values
+    mx = e.max(0, keepdim=True).values
+    ex = torch.exp((e - mn) / (mx - mn))
+    l = torch.zeros(N, H, dtype=e.dtype).index_add(0, rows, ex)
+    out = torch.zeros(N, H, Fo, dtype=e.dtype).index_add(0, rows, ex[:, :, None] * X1[col])
+    out = out / l[:, :, None]
+    return out if n_out is None else out[:n_out]
 
 
 def rel_err_fro(got, ref):

@@ -109,3 +109,55 @@ def test_fused_gat_training_lowers_loss(cuda):
         opt.step()
         losses.append(float(loss.detach()))
     assert all(np.isfinite(losses)) and min(losses[6:]) < losses[0], losses
+
+
+def test_gatv2_layer_forward_backward_vs_fp64(cuda):
+    """GATv2Conv_multi (end2end_head/gatv2_final/mgat_csr/mgat_conv.py:151-196)
+    over the drop-ins: output and the gradients of both projections and of
+    the attention vector against FP64 autograd of the oracle's restatement."""
+    from att_gb300 import layers
+    n, Fi, Fo, H = 700, 32, 32, 2
+    rows, cols, rp, col = _edges(n, 10, 6)
+    info = layers.GATInput(rows, cols, n)
+    torch.manual_seed(1)
+    conv = layers.GATv2Conv_multi(Fi, Fo, 0.0, 0.2, H).cuda()
+    X = (torch.rand(n, Fi, generator=torch.Generator().manual_seed(7)) - 0.5).half().cuda()
+    y = conv(X, info)
+    assert y.shape == (n, H, Fo)
+    G = torch.randn(n, H, Fo, generator=torch.Generator().manual_seed(8)).cuda()
+    (y.float() * G).sum().backward()
+    W0 = conv.fc0.weight.detach().t().half().double().cpu().requires_grad_(True)
+    W1 = conv.fc1.weight.detach().t().half().double().cpu().requires_grad_(True)
+    a = conv.a0.detach().half().double().cpu().requires_grad_(True)
+    ref = oracle.gatv2_layer_torch(rp, col, X.double().cpu(), W0, W1, a, 0.2)
+    (ref * G.double().cpu()).sum().backward()
+    assert oracle.rel_err(y.detach().float().cpu().numpy(), ref.detach().numpy()) <= 1e-2
+    for got, want in ((conv.fc0.weight.grad.t(), W0.grad), (conv.fc1.weight.grad.t(), W1.grad),
+                      (conv.a0.grad, a.grad)):
+        err = oracle.rel_err(got.float().cpu().numpy(), want.numpy())
+        assert err <= 2e-2, err
+
+
+def test_v4_attention_vector_helpers(cuda):
+    """ATT_SpMM_v4.bmm_v_m / bmm_v_v against their caller's math
+    (end2end_acc/gat_final/mgat_csr/mgat_conv.py:82,94), in both node-vector
+    layouts."""
+    from att_gb300.compat import ATT_SpMM_v4
+    g = torch.Generator().manual_seed(3)
+    h, M, F = 4, 300, 64
+    a0t = torch.randn(h, M, 1, generator=g).half().cuda()
+    a1t = torch.randn(h, M, 1, generator=g).half().cuda()
+    X = torch.randn(h, F, M, generator=g).half().cuda()
+    ta = torch.randn(h, 1, F, generator=g).half().cuda()
+    want0 = torch.einsum("hm,hfm->hf", a0t[..., 0].double(), X.double())[:, None, :]
+    want1 = torch.einsum("hm,hfm->hf", a1t[..., 0].double(), X.double())[:, None, :]
+    tg = a0t + a1t
+    want_v = (tg[..., 0].double().T[:, :, None] * ta[:, 0].double()[None]).reshape(M, h * F)
+    for lay in (lambda v: v, lambda v: v.transpose(1, 2).contiguous()):
+        g0, g1 = ATT_SpMM_v4.bmm_v_m(lay(a0t), lay(a1t), X)
+        assert g0.shape == (h, 1, F) and g1.shape == (h, 1, F)
+        assert oracle.rel_err(g0.double().cpu().numpy(), want0.cpu().numpy()) <= 1e-2
+        assert oracle.rel_err(g1.double().cpu().numpy(), want1.cpu().numpy()) <= 1e-2
+        v = ATT_SpMM_v4.bmm_v_v(lay(tg), ta)[0]
+        assert v.shape == (M, h * F)
+        assert oracle.rel_err(v.double().cpu().numpy(), want_v.cpu().numpy()) <= 1e-2

@@ -195,3 +195,17 @@ def test_gcn2_restatement_is_two_layers_of_spmm():
     h = np.maximum(oracle.spmm_csr_fp64(rp, col, vals, X @ W1), 0)
     want = oracle.spmm_csr_fp64(rp, col, vals, h @ W2)
     assert np.allclose(oracle.gcn2_fp64(rp, col, vals, X, W1, W2, n), want, atol=1e-12)
+
+
+def test_gatv2_restatement_gradients_by_finite_differences():
+    """The GATv2 restatement's autograd gradients agree with FP64 central
+    differences (torch.autograd.gradcheck) on a small graph."""
+    import torch
+    rp, col = _small_graph(seed=1, n=40)
+    g = torch.Generator().manual_seed(0)
+    X = torch.rand(40, 6, generator=g, dtype=torch.float64)
+    W0 = torch.rand(6, 8, generator=g, dtype=torch.float64).requires_grad_(True)
+    W1 = torch.rand(6, 8, generator=g, dtype=torch.float64).requires_grad_(True)
+    a = torch.rand(2, 1, 4, generator=g, dtype=torch.float64).requires_grad_(True)
+    assert torch.autograd.gradcheck(
+        lambda w0, w1, aa: oracle.gatv2_layer_torch(rp, col, X, w0, w1, aa), (W0, W1, a))

@@ -307,7 +307,8 @@ def test_autotune_spmm_picks_a_measured_shape(cuda, restore_spmm_options, dtype)
     """tune_spmm times every candidate shape and returns the fastest without
     changing the options in effect afterwards (read back through
     att_get_option); the chosen shape, passed per call, gives the default
-    shape's result (same arithmetic; atomics may reorder fp32 adds)."""
+    shape's result (same arithmetic; atomics may reorder fp32 adds), and the
+    next call without a shape is back at the defaults."""
     from att_gb300 import _lib, autotune, graphs, ops
     import ctypes
     rowptr, col = graphs.random_csr(2000, 2000, 25, seed=9, hub_rows=3, hub_len=1500)
@@ -339,8 +340,11 @@ def test_autotune_spmm_picks_a_measured_shape(cuda, restore_spmm_options, dtype)
     assert options() == before
     Y1 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale,
                   shape=choice)
-    assert options() == before
     assert oracle.rel_err(Y1.cpu().numpy(), Y0.cpu().numpy()) <= 1e-6
+    # a call without a shape runs (and leaves the thread) at the defaults
+    Y2 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale)
+    assert options() == before
+    assert oracle.rel_err(Y2.cpu().numpy(), Y0.cpu().numpy()) <= 1e-6
 
 
 @pytest.mark.parametrize("F", [64, 72, 128, 36])
