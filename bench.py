@@ -724,8 +724,9 @@ class ConvertProducts:
     name = "convert_products_fp16"
     unit = "GB/s"
     e2e_api = "Block_sr_bcrs.blockProcess_fp16_balance (host CSR in, host format out)"
-    kernel_name = ("att_block_plan + att_block_fill (k_unique_*, k_window_counts, scans, "
-                   "k_fill_structure, k_fill_edges)")
+    kernel_name = ("att_block_plan + att_block_fill (k_unique_warp, k_chunk_rows, k_merge_rank, "
+                   "scans, k_merge_emit, k_window_counts, k_fill_cols, k_fill_parts, "
+                   "k_fill_edges)")
 
     def __init__(self, device, scale=1.0, light=False):
         import torch
@@ -752,7 +753,7 @@ class ConvertProducts:
         self.bytes_alg = 4 * (rp.shape[0]) + 4 * self.nnz + 2 * rp.shape[0] + self.bytes_out
         self.bytes_compulsory = self.bytes_alg
         self.flops = 0
-        self.launches_per_step = 11
+        self.launches_per_step = 23  # plan 19 (its int32 scan 5 here) + fill 4
         self.config.update({"parts": f.n_parts, "condensed_cols": f.n_condensed,
                             "l2": "inputs and outputs larger than L2 (no flush)"})
 

@@ -55,7 +55,7 @@ def test_compat_module_returns_reference_tuple(cuda):
     assert res[4].tolist() == [1, 1, 0, 1, 1, 0]
 
 
-@pytest.mark.parametrize("case", range(6))
+@pytest.mark.parametrize("case", range(10))
 def test_random_graphs_vs_oracle_with_maps(cuda, case):
     from att_gb300 import graphs
     specs = [
@@ -65,6 +65,15 @@ def test_random_graphs_vs_oracle_with_maps(cuda, case):
         dict(n_rows=129, n_cols=2000, max_len=40, seed=4, dup=True, sort_rows=False),
         dict(n_rows=64, n_cols=9000, max_len=3, seed=5, hub_rows=4, hub_len=5000),  # > smem cap
         dict(n_rows=1001, n_cols=1001, max_len=30, seed=6, hub_rows=1, hub_len=1000),
+        # windows of tens of thousands of edges through the merge path
+        dict(n_rows=48, n_cols=300000, max_len=20, seed=7, hub_rows=3, hub_len=45000),
+        # unsorted rows with duplicates in windows of 1025..4096 edges and of
+        # more than 4096 (the sorting and bitmap fallbacks of the merge path)
+        dict(n_rows=80, n_cols=5000, max_len=300, seed=8, dup=True, sort_rows=False),
+        dict(n_rows=40, n_cols=60000, max_len=5, seed=9, hub_rows=2, hub_len=40000, dup=True,
+             sort_rows=False),
+        # sorted rows with repeated columns, in windows of a few hundred edges
+        dict(n_rows=64, n_cols=3000, max_len=200, seed=10, dup=True),
     ]
     sp = specs[case]
     rowptr, col = graphs.random_csr(**sp)
