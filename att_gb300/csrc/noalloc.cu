@@ -13,14 +13,18 @@
 // Host code cannot use the array's name as a device address (on the host it is
 // only a stand-in symbol), so the address is looked up once per device with
 // cudaGetSymbolAddress while that device is current, checked, cached, and then
-// passed to the kernels.  The first call on a device performs this set-up, so
-// make that first call before any stream capture begins.
+// passed to the kernels.  The first call on a device performs this set-up.
+// The cached address is not refreshed after cudaDeviceReset: a process that
+// resets a device must not call this entry point afterwards.
 //
+// The call returns only when its GPU work is done (the plan synchronises the
+// stream to read the sizes, the fill to read the device-side checks), so it
+// cannot be captured into a CUDA graph and successive calls never overlap.
 // All calls share the one array and it keeps the previous call's contents:
 // everything the kernels read is cleared or rewritten by the call itself
-// (flags and per-window counts are zeroed, the column bitmap is cleared per
-// window).  Calls whose GPU work overlaps -- on two streams, or from two host
-// threads -- race on the array; callers must order them.
+// (flags, per-window counts and bitmaps are zeroed, merge flags cleared).
+// Calls from two host threads at the same time race on the array; callers
+// must order them.
 #include "att_common.cuh"
 
 #include <mutex>

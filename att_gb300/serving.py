@@ -10,10 +10,12 @@ request loop:
   estimate of the admitted set stays within the HBM budget and a slot is free;
   a request larger than the whole budget, or whose graph fails validation, is
   rejected with an error instead of blocking the queue;
-* preparation -- a worker thread per slot, each on its own CUDA stream, uploads
-  the CSR and features, converts the graph to the block format on the GPU,
-  builds its deterministic work groups (att_spmm_groups) and projects X W1;
-  the format and features then stay resident until the request completes;
+* preparation -- the one host thread that drives the loop enqueues each
+  admitted request on one of two preparation streams, without blocking: it
+  uploads the CSR and features, converts the graph to the block format on the
+  GPU (the plan's sizes come back through pinned memory and an event), builds
+  its deterministic work groups (att_spmm_groups) and projects X W1; the
+  format and features then stay resident until the request completes;
 * aggregation -- every scheduler tick packs the row windows of *all* requests
   that are ready for an aggregation (layer 1 or layer 2) into one batched SpMM
   (att_spmm_batched), replayed from a captured CUDA graph whose kernels read a

@@ -160,10 +160,14 @@ ATT_API int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t n_
  *     max_condensed are their capacities (in parts and condensed columns).
  *     The sizes are written to n_parts_out / n_condensed_out; if they exceed
  *     the capacities the call returns ATT_ERR_WORKSPACE before writing.
- *   - The first call on a device looks up the array's device address; make
- *     it before any stream capture starts.
- *   - All calls share the array: calls whose GPU work overlaps race.
- *   - Synchronises `stream` (to read the sizes), like att_block_plan.
+ *   - The first call on a device looks up the array's device address and
+ *     keeps it for the life of the process; the kept address does not
+ *     survive cudaDeviceReset (do not call this after resetting a device).
+ *   - The call blocks until its GPU work is done (it synchronises `stream`
+ *     to read the sizes and again to read the device-side checks), so it
+ *     cannot be used inside a stream capture, and calls made one after the
+ *     other never overlap.  All calls share the array: calls from different
+ *     host threads at the same time race on it -- the caller orders them.
  * ---------------------------------------------------------------------- */
 ATT_API size_t att_block_convert_noalloc_max_scratch(void);
 ATT_API int att_block_convert_noalloc(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
