@@ -46,6 +46,8 @@ _SIGNATURES = {
     "att_spmm": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_i64, _c_vp, _c_int,
                           _c_vp, _c_i64, _c_i64, _c_i64, _c_vp, _c_i64, _c_i64, _c_int, _c_int,
                           _c_vp, _c_vp]),
+    "att_node_scores_pair": (_c_int, [_c_vp, _c_int, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64,
+                                      _c_vp, _c_vp, _c_i64, _c_vp, _c_vp, _c_i64, _c_vp]),
     "att_node_scores": (_c_int, [_c_vp, _c_int, _c_i64, _c_i64, _c_i64, _c_i64, _c_i64, _c_vp,
                                  _c_int, _c_i64, _c_vp, _c_i64, _c_vp]),
     "att_slot_edges": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_i64, _c_int, _c_int, _c_int,

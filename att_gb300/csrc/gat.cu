@@ -72,6 +72,48 @@ __global__ void k_node_scores(const void *__restrict__ X, int xdt, int64_t H, in
     if (lane == 0) s[h * ssh + m] = acc;
 }
 
+// s0[h][m] = X[h][m] . a0[h] and s1[h][m] = X[h][m] . a1[h] in one pass over X
+// (16-bit X, fp32 attention vectors): LPR = F / 8 lanes per node row, each
+// loading 8 features with one 16-byte load; the row's partial sums meet by
+// shuffles within its lanes.
+template <typename T, int LPR>
+__global__ void k_node_scores_pair(const T *__restrict__ X, int64_t H, int64_t M, int64_t xsh,
+                                   int64_t xsm, const float *__restrict__ a0,
+                                   const float *__restrict__ a1, int64_t ash,
+                                   float *__restrict__ s0, float *__restrict__ s1, int64_t ssh) {
+    constexpr int RPW = 32 / LPR;  // node rows per warp
+    const int lane = threadIdx.x & 31, sub = lane % LPR;
+    const int64_t row = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * RPW + lane / LPR;
+    const bool ok = row < H * M;
+    const int64_t h = ok ? row / M : 0, m = ok ? row - h * M : 0;
+    float acc0 = 0.f, acc1 = 0.f;
+    if (ok) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(X + h * xsh + m * xsm + sub * 8);
+        const T *x = reinterpret_cast<const T *>(&v);
+        const float4 p0 = *reinterpret_cast<const float4 *>(a0 + h * ash + sub * 8);
+        const float4 q0 = *reinterpret_cast<const float4 *>(a0 + h * ash + sub * 8 + 4);
+        const float4 p1 = *reinterpret_cast<const float4 *>(a1 + h * ash + sub * 8);
+        const float4 q1 = *reinterpret_cast<const float4 *>(a1 + h * ash + sub * 8 + 4);
+        const float w0[8] = {p0.x, p0.y, p0.z, p0.w, q0.x, q0.y, q0.z, q0.w};
+        const float w1[8] = {p1.x, p1.y, p1.z, p1.w, q1.x, q1.y, q1.z, q1.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float xv = ld_f<T>(x, k);
+            acc0 += xv * w0[k];
+            acc1 += xv * w1[k];
+        }
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {
+        acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
+        acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
+    }
+    if (ok && sub == 0) {
+        s0[h * ssh + m] = acc0;
+        s1[h * ssh + m] = acc1;
+    }
+}
+
 // ---- per-slot edge values -----------------------------------------------------
 // mode 0: out[e] = s0[row] + s1[col]      mode 1: out[e] = g[row]
 struct SlotEdgeArgs {
@@ -575,6 +617,49 @@ extern "C" int att_node_scores(const void *X, int x_dtype, int64_t n_heads, int6
         X, x_dtype, n_heads, n_nodes, F, x_stride_h, x_stride_n, a, a_dtype, a_stride_h, scores,
         s_stride_h);
     return launch_status("k_node_scores");
+}
+
+extern "C" int att_node_scores_pair(const void *X, int x_dtype, int64_t n_heads, int64_t n_nodes,
+                                    int64_t F, int64_t x_stride_h, int64_t x_stride_n,
+                                    const float *a0, const float *a1, int64_t a_stride_h,
+                                    float *s0, float *s1, int64_t s_stride_h, void *stream) {
+    clear_error();
+    ATT_CHECK(n_heads >= 0 && n_nodes >= 0 && F >= 0, ATT_ERR_INVALID, "negative size");
+    const int64_t rows = n_heads * n_nodes;
+    if (rows == 0) return ATT_OK;
+    ATT_CHECK(X && a0 && a1 && s0 && s1, ATT_ERR_INVALID, "null pointer");
+    const bool v16 = (x_dtype == ATT_F16 || x_dtype == ATT_BF16) &&
+                     (F == 8 || F == 16 || F == 32 || F == 64 || F == 128 || F == 256) &&
+                     x_stride_h % 8 == 0 && x_stride_n % 8 == 0 && ((uintptr_t)X & 15) == 0 &&
+                     a_stride_h % 8 == 0 && ((uintptr_t)a0 & 15) == 0 && ((uintptr_t)a1 & 15) == 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!v16) {  // any layout: two passes of the generic kernel
+        int s = att_node_scores(X, x_dtype, n_heads, n_nodes, F, x_stride_h, x_stride_n, a0,
+                                ATT_F32, a_stride_h, s0, s_stride_h, stream);
+        if (s != ATT_OK) return s;
+        return att_node_scores(X, x_dtype, n_heads, n_nodes, F, x_stride_h, x_stride_n, a1,
+                               ATT_F32, a_stride_h, s1, s_stride_h, stream);
+    }
+    const int lpr = (int)(F / 8);
+    const int64_t warps = (rows * lpr + 31) / 32;
+    const unsigned grid = (unsigned)((warps * 32 + 255) / 256);
+#define ATT_NSP(T, L)                                                                           \
+    k_node_scores_pair<T, L><<<grid, 256, 0, st>>>((const T *)X, n_heads, n_nodes, x_stride_h, \
+                                                   x_stride_n, a0, a1, a_stride_h, s0, s1,     \
+                                                   s_stride_h)
+#define ATT_NSP_T(T)                                  \
+    switch (lpr) {                                    \
+        case 1: ATT_NSP(T, 1); break;                 \
+        case 2: ATT_NSP(T, 2); break;                 \
+        case 4: ATT_NSP(T, 4); break;                 \
+        case 8: ATT_NSP(T, 8); break;                 \
+        case 16: ATT_NSP(T, 16); break;               \
+        default: ATT_NSP(T, 32); break;               \
+    }
+    if (x_dtype == ATT_F16) { ATT_NSP_T(__half) } else { ATT_NSP_T(__nv_bfloat16) }
+#undef ATT_NSP_T
+#undef ATT_NSP
+    return launch_status("k_node_scores_pair");
 }
 
 extern "C" int att_slot_edges(const int32_t *rowptr, const int32_t *col, const int32_t *map,

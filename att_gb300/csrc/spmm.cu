@@ -1767,33 +1767,53 @@ __global__ void k_empty_scatter(const int32_t *__restrict__ win, int64_t P, int6
     if (w == n_windows - 1) counts[3] = scanned[w] + empty;
 }
 
-// Zero the output rows that no unsplit part writes: rows of split windows,
-// of windows without parts and rows past the last window.  Each thread looks
-// up one window (binary search of the sorted window ids); the warp then zeroes
-// the windows that need it together, one row at a time across its lanes.
+// Outputs up to this size are zeroed whole before the SpMM kernel (one
+// memset, a few microseconds); larger ones by k_zero_uncovered.
+constexpr size_t kZeroAllBytes = 32ull << 20;
+
+// Zeroes the rows of Y that no unsplit part stores (windows whose parts add
+// with red.add, windows without parts, rows past the last window), before
+// the SpMM kernel.  Thread per part, plus one thread for the end: the first
+// part of each window zeroes the windows between the previous part's window
+// and its own, and its own window when that window is split; the extra
+// thread zeroes the windows after the last part's.  No searches: every
+// thread reads at most two window ids and one flag, coalesced.  The warp
+// zeroes each lane's rows together.
 __global__ void k_zero_uncovered(const int32_t *__restrict__ win, const int32_t *__restrict__ atomic,
                                  int64_t n_parts, int W, float *__restrict__ Y, int64_t m_out,
                                  int64_t F, int64_t ldy) {
     const int lane = threadIdx.x & 31;
     const int64_t n_w = (m_out + W - 1) / W;
-    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool need = false;
-    if (w < n_w) {
-        int64_t lo = 0, hi = n_parts;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if (__ldg(win + mid) < w) lo = mid + 1; else hi = mid;
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t g0 = 0, g1 = 0, own = -1;  // gap [g0, g1) and the own window to zero
+    if (p < n_parts) {
+        const int64_t w = __ldg(win + p);
+        const int64_t prev = p > 0 ? (int64_t)__ldg(win + p - 1) : -1;
+        if (prev != w) {
+            g0 = prev + 1;
+            g1 = w;
+            if (__ldg(atomic + p) != 0) own = w;
         }
-        need = !(lo < n_parts && __ldg(win + lo) == w && __ldg(atomic + lo) == 0);
+    } else if (p == n_parts) {
+        g0 = n_parts > 0 ? (int64_t)__ldg(win + n_parts - 1) + 1 : 0;
+        g1 = n_w;
     }
-    unsigned m = __ballot_sync(0xffffffffu, need);
+    g0 = g0 < 0 ? 0 : g0;
+    g1 = g1 > n_w ? n_w : g1;
+    if (own >= n_w) own = -1;
+    unsigned m = __ballot_sync(0xffffffffu, g1 > g0 || own >= 0);
     while (m) {
         const int l = __ffs(m) - 1;
         m &= m - 1;
-        const int64_t ww = w - lane + l;
-        const int64_t r1 = (ww + 1) * W < m_out ? (ww + 1) * W : m_out;
-        for (int64_t r = ww * W; r < r1; ++r)
-            for (int64_t f = lane; f < F; f += 32) Y[r * ldy + f] = 0.f;
+        const int64_t lg0 = __shfl_sync(0xffffffffu, g0, l), lg1 = __shfl_sync(0xffffffffu, g1, l);
+        const int64_t lown = __shfl_sync(0xffffffffu, own, l);
+        for (int pass = 0; pass < 2; ++pass) {
+            const int64_t w0 = pass == 0 ? lg0 : lown, w1 = pass == 0 ? lg1 : lown + 1;
+            if (w1 <= w0 || w0 < 0) continue;
+            const int64_t r1 = w1 * W < m_out ? w1 * W : m_out;
+            for (int64_t r = w0 * W; r < r1; ++r)
+                for (int64_t f = lane; f < F; f += 32) Y[r * ldy + f] = 0.f;
+        }
     }
 }
 
@@ -2110,8 +2130,13 @@ extern "C" int att_spmm(const int32_t *rowptr, const int32_t *col, const void *v
     cudaStream_t st = (cudaStream_t)stream;
     if (m_out == 0 || F == 0) return ATT_OK;
     int s = ATT_OK;
-    {
-        int64_t threads = (m_out + window - 1) / window;
+    if ((size_t)m_out * (size_t)ldy * sizeof(float) <= kZeroAllBytes) {
+        // a small Y: zeroing all of it costs less than finding what to zero
+        ATT_CUDA(cudaMemset2DAsync(Y, (size_t)ldy * sizeof(float), 0, (size_t)F * sizeof(float),
+                                   (size_t)m_out, st),
+                 "zero Y");
+    } else {
+        const int64_t threads = n_parts + 1;
         k_zero_uncovered<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
             window_of_part, atomic, n_parts, window, Y, m_out, F, ldy);
         s = launch_status("k_zero_uncovered");

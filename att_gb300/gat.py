@@ -177,8 +177,7 @@ class GATAttention(torch.autograd.Function):
         F = Xp.shape[1] // n_heads
         X3 = Xp.view(N, n_heads, F).permute(1, 0, 2)
         # attention vectors stay fp32: rounding them would shift every score
-        s0 = gat_ops.node_scores(X3, a0.float())
-        s1 = gat_ops.node_scores(X3, a1.float())
+        s0, s1 = gat_ops.node_scores_pair(X3, a0, a1)
         out, rmax, rsum = graph.attention(Xp, n_heads=n_heads, mode=MODE_ADD, s0=s0, s1=s1,
                                           slope=slope)
         ctx.save_for_backward(Xp, a0, a1, s0, s1, rmax, rsum, out)

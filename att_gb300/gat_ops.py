@@ -55,6 +55,21 @@ def node_scores(X3, a2):
     return s
 
 
+def node_scores_pair(X3, a0, a1):
+    """(s0, s1) with s0[h][m] = X3[h, m, :] . a0[h, :] and s1 likewise, fp32,
+    in one pass over X3 [H, M, F]; a0 / a1 [H, F] (used as fp32)."""
+    require_cuda()
+    H, M, F = X3.shape
+    if X3.stride(2) != 1:
+        X3 = X3.contiguous()
+    a0 = a0.float().contiguous()
+    a1 = a1.float().contiguous()
+    s = torch.empty(2, H, M, dtype=torch.float32, device=X3.device)
+    _lib.call("att_node_scores_pair", _p(X3), _DT[X3.dtype], H, M, F, X3.stride(0), X3.stride(1),
+              _p(a0), _p(a1), a0.stride(0), _p(s[0]), _p(s[1]), s.stride(1), _stream())
+    return s[0], s[1]
+
+
 def _edge_out(H, nnz, dtype, device, layout):
     if layout == "h_e":
         out = torch.zeros(H, nnz, dtype=dtype, device=device)

@@ -226,6 +226,15 @@ ATT_API int att_node_scores(const void *X, int x_dtype, int64_t n_heads, int64_t
                    int64_t F, int64_t x_stride_h, int64_t x_stride_n, const void *a,
                    int a_dtype, int64_t a_stride_h, float *scores, int64_t s_stride_h,
                    void *stream);
+/* s0[h][m] = X[h][m] . a0[h] and s1[h][m] = X[h][m] . a1[h] in one pass over
+ * X (fp32 attention vectors a0 / a1 [h][F] with row stride a_stride_h).
+ * No counterpart in the reference: the fused GAT layer's two node-score
+ * vectors, the building block of att_*_h_nnz computed once per node instead
+ * of per edge. */
+ATT_API int att_node_scores_pair(const void *X, int x_dtype, int64_t n_heads, int64_t n_nodes,
+                   int64_t F, int64_t x_stride_h, int64_t x_stride_n, const float *a0,
+                   const float *a1, int64_t a_stride_h, float *s0, float *s1,
+                   int64_t s_stride_h, void *stream);
 
 /* For every slot with an edge e (row i = window*W + r, column j = col[c]):
  *   mode 0: out[h][e] = s0[h][i] + s1[h][j]   (att_*_h_nnz: X_i.a0 + X_j.a1;

@@ -228,3 +228,27 @@ def test_edge_softmax_vs_fp64(cuda, odt, H):
         assert np.allclose(rm[has], m_ref[has], rtol=1e-6, atol=0)
         assert np.allclose(rs[has], s_ref[has], rtol=1e-5, atol=0)
         assert np.all(np.isneginf(rm[~has])) and np.all(rs[~has] == 0)
+
+
+@pytest.mark.parametrize("dtype", [torch.float16, torch.bfloat16, torch.float32])
+@pytest.mark.parametrize("H,F", [(1, 8), (4, 64), (2, 128), (1, 256), (3, 40)])
+def test_node_scores_pair_matches_two_single_passes(cuda, dtype, H, F):
+    """att_node_scores_pair (one pass, 16-byte loads where the layout allows)
+    against two att_node_scores passes and FP64, on the [H, N, F] view of an
+    [N, H*F] projection (the fused GAT layer's layout)."""
+    from att_gb300 import gat_ops
+    g = torch.Generator().manual_seed(H * 1000 + F)
+    n = 1237
+    Xp = (torch.rand(n, H * F, generator=g) * 2 - 1).to(dtype).cuda()
+    X3 = Xp.view(n, H, F).permute(1, 0, 2)
+    a0 = (torch.rand(H, F, generator=g) - 0.5).cuda()
+    a1 = (torch.rand(H, F, generator=g) - 0.5).cuda()
+    s0, s1 = gat_ops.node_scores_pair(X3, a0, a1)
+    r0 = gat_ops.node_scores(X3, a0)
+    r1 = gat_ops.node_scores(X3, a1)
+    ref0 = torch.einsum("hmf,hf->hm", X3.double(), a0.double())
+    ref1 = torch.einsum("hmf,hf->hm", X3.double(), a1.double())
+    for got, single, ref in ((s0, r0, ref0), (s1, r1, ref1)):
+        assert got.shape == (H, n)
+        assert oracle.rel_err(got.cpu().numpy(), ref.cpu().numpy()) <= 1e-5
+        assert oracle.rel_err(got.cpu().numpy(), single.cpu().numpy()) <= 1e-5
