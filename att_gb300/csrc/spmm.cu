@@ -1112,14 +1112,27 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8(
 // Same staging ring as k_spmm_fp8, without the fp16 tile: ldmatrix.trans
 // reads the e4m3 rows as 16-bit feature pairs, so each register holds
 // features (f, f+1) of two gathered rows (c, c+1).  One byte permute regroups
-// it into (f: c, c+1) | (f+1: c, c+1), two cvt.e4m3x2 -> f16x2 give the A
-// fragments of two MMA rows, and one multiply by the rows' scale pair applies
-// the per-row scales.  The MMA rows are thereby a permutation of the features
-// (row m < 8 is feature 2m of its 16-feature tile, row m + 8 is feature
-// 2m + 1), which the epilogue undoes: each lane ends up owning two adjacent
-// features of two window rows and stores them as float2.  This removes the
-// shared-memory round trip of the fp16 tile (4 KB of shared traffic and four
-// 16-byte stores per lane per step) and lets one work item cover 128 features.
+// it into (f: c, c+1) | (f+1: c, c+1), and two cvt.e4m3x2 -> f16x2 give the A
+// fragments of two MMA rows.  The per-row scales are folded into the B
+// fragment (the step's block values, 16 gathered rows x 8 or 16 window rows):
+// B' = fp16(V * s * 2^15), a few multiplies per step instead of one per A
+// register, and the fp32 accumulators are multiplied by 2^-15 at the store
+// (both factors are powers of two, so exact).  A step whose scaled values
+// would leave fp16's normal range scales A by fp16(s) instead.  The MMA rows
+// are a permutation of the features (row m < 8 is feature 2m of its
+// 16-feature tile, row m + 8 is feature 2m + 1), which the epilogue undoes:
+// each lane ends up owning two adjacent features of two window rows and
+// stores them as float2.  This removes the shared-memory round trip of the
+// fp16 tile (4 KB of shared traffic and four 16-byte stores per lane per
+// step) and lets one work item cover 128 features.
+constexpr float kF8Shift = 32768.f;
+constexpr float kF8Unshift = 1.f / 32768.f;
+
+__device__ __forceinline__ bool f16_normal_or_zero(float x) {
+    const float a = fabsf(x);
+    return a == 0.f || (a >= 6.103515625e-05f && a <= 65504.f);
+}
+
 template <int W, int FC, int S = kF8Stages>
 struct CfgF8R {
     static constexpr int XROW = FC;              // bytes per gathered e4m3 row
@@ -1257,8 +1270,6 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
             // rows (2 tig, 2 tig + 1) and (8 + 2 tig, 9 + 2 tig)
             const float2 s_lo = *reinterpret_cast<const float2 *>(sc + 2 * tig);
             const float2 s_hi = *reinterpret_cast<const float2 *>(sc + 8 + 2 * tig);
-            const __half2 h_lo = __floats2half2_rn(s_lo.x, s_lo.y);
-            const __half2 h_hi = __floats2half2_rn(s_hi.x, s_hi.y);
             uint32_t b[C::NT][2];
             {
                 const int q = lane >> 3, rr = lane & 7;
@@ -1272,6 +1283,40 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
                     ldsm_x2(vs + e * 2, b[0][0], b[0][1]);
                 }
             }
+            // The row scales go on the B fragment: b[t][0] holds the values of
+            // gathered rows (2 tig, 2 tig + 1), b[t][1] of (8 + 2 tig, 9 + 2 tig),
+            // exactly the rows of the lane's scale pairs.  V * s is multiplied
+            // by kF8Shift (2^15) into fp16's normal range, so the accumulators
+            // hold 2^15 * Y until the store; if any scaled value of the step
+            // would be neither zero nor a normal fp16, the warp scales A
+            // instead for that step (accumulators brought back to 1 * Y around
+            // it, exact: powers of two).
+            uint32_t bs[C::NT][2];
+            bool ok = true;
+#pragma unroll
+            for (int t = 0; t < C::NT; ++t) {
+#pragma unroll
+                for (int g = 0; g < 2; ++g) {
+                    const float2 v = __half22float2(*reinterpret_cast<const __half2 *>(&b[t][g]));
+                    const float2 sg = g == 0 ? s_lo : s_hi;
+                    const float p0 = v.x * sg.x * kF8Shift, p1 = v.y * sg.y * kF8Shift;
+                    ok = ok && f16_normal_or_zero(p0) && f16_normal_or_zero(p1);
+                    const __half2 hp = __floats2half2_rn(p0, p1);
+                    bs[t][g] = *reinterpret_cast<const uint32_t *>(&hp);
+                }
+            }
+            const bool bside = __all_sync(0xffffffffu, ok);
+            __half2 h_lo, h_hi;
+            if (!bside) {
+                h_lo = __floats2half2_rn(s_lo.x, s_lo.y);
+                h_hi = __floats2half2_rn(s_hi.x, s_hi.y);
+#pragma unroll
+                for (int j = 0; j < C::MT; ++j)
+#pragma unroll
+                    for (int t = 0; t < C::NT; ++t)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[j][t][q] *= kF8Unshift;
+            }
 #pragma unroll
             for (int jp = 0; jp < C::MT / 2; ++jp) {
                 const int ch = 2 * jp + lm_h;
@@ -1284,14 +1329,32 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
                     const uint32_t p0 = __byte_perm(R[h], 0, 0x3120);      // rows 2tig, 2tig+1
                     const uint32_t p1 = __byte_perm(R[h + 2], 0, 0x3120);  // rows 8+2tig, 9+2tig
                     uint32_t a[4];
-                    a[0] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p0 & 0xffffu)), h_lo);
-                    a[1] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p0 >> 16)), h_lo);
-                    a[2] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p1 & 0xffffu)), h_hi);
-                    a[3] = hmul2_u32(e4m3x2_to_f16x2((uint16_t)(p1 >> 16)), h_hi);
+                    a[0] = e4m3x2_to_f16x2((uint16_t)(p0 & 0xffffu));
+                    a[1] = e4m3x2_to_f16x2((uint16_t)(p0 >> 16));
+                    a[2] = e4m3x2_to_f16x2((uint16_t)(p1 & 0xffffu));
+                    a[3] = e4m3x2_to_f16x2((uint16_t)(p1 >> 16));
+                    if (bside) {
+#pragma unroll
+                        for (int t = 0; t < C::NT; ++t)
+                            mma_16816<__half>(acc[2 * jp + h][t], a, bs[t][0], bs[t][1]);
+                    } else {
+                        a[0] = hmul2_u32(a[0], h_lo);
+                        a[1] = hmul2_u32(a[1], h_lo);
+                        a[2] = hmul2_u32(a[2], h_hi);
+                        a[3] = hmul2_u32(a[3], h_hi);
+#pragma unroll
+                        for (int t = 0; t < C::NT; ++t)
+                            mma_16816<__half>(acc[2 * jp + h][t], a, b[t][0], b[t][1]);
+                    }
+                }
+            }
+            if (!bside) {
+#pragma unroll
+                for (int j = 0; j < C::MT; ++j)
 #pragma unroll
                     for (int t = 0; t < C::NT; ++t)
-                        mma_16816<__half>(acc[2 * jp + h][t], a, b[t][0], b[t][1]);
-                }
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[j][t][q] *= kF8Shift;
             }
             __syncwarp();
             if (p_item < n_items) {
@@ -1317,7 +1380,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_fp8r(
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const IT r = r0 + h;
-                    const float v0 = acc[j][t][h], v1 = acc[j][t][h + 2];
+                    const float v0 = acc[j][t][h] * kF8Unshift, v1 = acc[j][t][h + 2] * kF8Unshift;
                     if (r < m_out && (FULL || f < F)) {
                         float *dst = Y + (r * ldy + f);
                         if (add) {
