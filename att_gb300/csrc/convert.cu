@@ -9,10 +9,10 @@
 // pipeline:
 //
 //   plan  k_unique_warp    one warp per window of <= kWarpCap edges: bitonic
-//                          sort of (column, edge index) keys in the warp's own
-//                          slice of shared memory, de-duplicate, warp-scan
-//                          compact; each edge's rank among its window's
-//                          distinct columns falls out of the sort
+//                          sort of (column, edge index) keys in registers,
+//                          de-duplicate, warp-scan compact; each edge's rank
+//                          among its window's distinct columns falls out of
+//                          the sort
 //         k_chunk_rows     row holding the first edge of each 2048-edge chunk
 //         k_merge_rank     larger windows, thread per edge: its position in
 //                          the merge of the window's sorted rows (binary
@@ -237,10 +237,95 @@ __device__ __forceinline__ void warp_bitonic(KT *keys, int n, int lane) {
     }
 }
 
-// Windows of LO+1 .. CAP edges: one warp each, sorted in the warp's own slice
-// of shared memory (warp-synchronous, no block barriers), then de-duplicated
-// and compacted with a warp scan; the rank of every edge's column is written
-// to erank.  With `unsorted_only`, only windows the merge path flagged.
+// Bitonic sort (ascending) of 32 * PER keys held by a warp in registers: key
+// i = lane * PER + q sits in v[q].  Compare distances below PER swap
+// registers of one lane; larger ones exchange with lane ^ (distance / PER).
+template <typename KT, int PER>
+__device__ __forceinline__ void warp_bitonic_regs(KT (&v)[PER], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * PER; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j < PER) {
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    if ((q & j) == 0) {
+                        const bool asc = ((lane * PER + q) & k) == 0;
+                        const KT x = v[q], y = v[q + j];
+                        const bool sw = asc ? (x > y) : (x < y);
+                        v[q] = sw ? y : x;
+                        v[q + j] = sw ? x : y;
+                    }
+                }
+            } else {
+                const int lj = j / PER;
+                const bool lower = (lane & lj) == 0;
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const bool asc = ((lane * PER + q) & k) == 0;
+                    const KT o = __shfl_xor_sync(0xffffffffu, v[q], lj);
+                    const KT mn = v[q] < o ? v[q] : o, mx = v[q] < o ? o : v[q];
+                    v[q] = lower == asc ? mn : mx;
+                }
+            }
+        }
+    }
+}
+
+// One window of 1 .. 32 * PER edges by the calling warp, in registers: sort
+// the (column, edge) keys, then each lane de-duplicates its PER consecutive
+// sorted keys (the key before its first comes from the lane below), a warp
+// scan places the distinct columns, and every edge gets its column's rank.
+template <typename KT, int PER, int IB>
+__device__ __forceinline__ void unique_window_regs(const int32_t *__restrict__ col, int64_t b0,
+                                                   int E, int64_t n_cols, const Workspace &ws,
+                                                   int64_t w, int lane) {
+    KT v[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int t = lane * PER + q;
+        v[q] = key_sentinel<KT>();
+        if (t < E) {
+            const int c = col[b0 + t];
+            if (c < 0 || c >= n_cols) atomicOr(ws.flags, FLAG_BAD_COL);
+            else v[q] = ((KT)c << IB) | (KT)t;
+        }
+    }
+    warp_bitonic_regs<KT, PER>(v, lane);
+    const KT below = __shfl_up_sync(0xffffffffu, v[PER - 1], 1);
+    bool fl[PER];
+    int cnt = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const KT prv = q == 0 ? below : v[q - 1];
+        fl[q] = v[q] != key_sentinel<KT>() &&
+                ((lane == 0 && q == 0) || (prv >> IB) != (v[q] >> IB));
+        cnt += fl[q] ? 1 : 0;
+    }
+    int x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, x, 31);
+    int pos = x - cnt;  // distinct columns before this lane's keys
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        if (v[q] != key_sentinel<KT>()) {
+            if (fl[q]) ws.ucols[b0 + pos++] = (int32_t)(v[q] >> IB);
+            ws.erank[b0 + (int64_t)(v[q] & (KT)((1u << IB) - 1))] = pos - 1;
+        }
+    }
+    if (lane == 0) ws.ucount[w] = total;
+}
+
+// Windows of LO+1 .. CAP edges: one warp each.  Up to kWarpCap edges the keys
+// sort in registers (unique_window_regs); larger windows sort in the warp's
+// own slice of shared memory (warp-synchronous, no block barriers).  Then the
+// window is de-duplicated and compacted with a warp scan; the rank of every
+// edge's column is written to erank.  With `unsorted_only`, only windows the
+// merge path flagged.
 constexpr int kWarpSortWarps = 8;
 constexpr int kWarpCap = 256;  // windows up to this many edges: warp sort; above: merge
 constexpr int kMidCap = 1024;
@@ -262,6 +347,13 @@ __global__ void __launch_bounds__(kWarpSortWarps * 32) k_unique_warp(
         window_range(rowptr, w, window, nnz, &b0, &b1, ws.flags);
         const int64_t E = b1 - b0;
         if (E > CAP || E <= LO) continue;  // another kernel's window
+        if constexpr (CAP == kWarpCap) {
+            if (E <= 32) unique_window_regs<KT, 1, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+            else if (E <= 64) unique_window_regs<KT, 2, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+            else if (E <= 128) unique_window_regs<KT, 4, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+            else unique_window_regs<KT, 8, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+            continue;
+        }
         int n = 32;
         while (n < E) n <<= 1;
         for (int t = lane; t < n; t += 32) {
@@ -583,20 +675,73 @@ __global__ void k_chunk_rows(const int32_t *__restrict__ rowptr, int64_t n_rows_
 
 // The edge-chunk kernels run a CTA of kEdgeThreads threads per kEdgeChunk CSR
 // edges of the used rows.  A chunk's rows run from the row of its first edge
-// to the row of the next chunk's first edge; that slice of rowptr is staged
-// in shared memory when it fits, so each edge finds its row with a short
-// search.
+// to the row of the next chunk's first edge.  When that slice of rowptr fits
+// in shared memory, the CTA builds the row of every edge of the chunk there
+// (EdgeRows): each row marks its first edge inside the chunk, and a max-scan
+// carries the mark over the row's edges.  Otherwise each edge searches
+// rowptr.
 constexpr int kEdgeThreads = 256;
 constexpr int kEdgeStage = 2048;
+constexpr int kEdgePer = kEdgeChunk / kEdgeThreads;  // scan entries per thread
+static_assert(kEdgePer == 8, "EdgeRows scans two int4 per thread");
 
 struct EdgeChunk {
     int64_t eb, ee, r0, r1, nr;
     bool staged;
 };
 
+struct EdgeRows {
+    int32_t rp[kEdgeStage];                    // rowptr[r0 .. r0 + nr - 1]
+    __align__(16) int32_t row[kEdgeChunk];     // row of edge eb + j, minus r0
+    int warp_max[kEdgeThreads / 32];
+};
+
+// Row of every edge of a staged chunk.  A row's first edge inside the chunk
+// (edge eb for rows starting at or before it) gets the row's index; the
+// largest index wins, so an empty row loses to the non-empty row sharing its
+// start.  An inclusive max-scan then gives every edge the last row that
+// starts at or before it, which is the row holding it.
+__device__ __forceinline__ void edge_rows_build(EdgeRows &sh, const EdgeChunk &c) {
+    const int len = (int)(c.ee - c.eb);
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    int4 *row4 = reinterpret_cast<int4 *>(sh.row);
+    for (int j = t; j < kEdgeChunk / 4; j += kEdgeThreads)
+        row4[j] = make_int4(j == 0 ? 0 : -1, -1, -1, -1);
+    __syncthreads();
+    for (int i = t; i < (int)c.nr; i += kEdgeThreads) {
+        const int64_t st = (int64_t)sh.rp[i] - c.eb;
+        if (st < len) atomicMax(&sh.row[st > 0 ? st : 0], i);
+    }
+    __syncthreads();
+    int4 lo = row4[2 * t], hi = row4[2 * t + 1];
+    lo.y = max(lo.y, lo.x);
+    lo.z = max(lo.z, lo.y);
+    lo.w = max(lo.w, lo.z);
+    hi.x = max(hi.x, lo.w);
+    hi.y = max(hi.y, hi.x);
+    hi.z = max(hi.z, hi.y);
+    hi.w = max(hi.w, hi.z);
+    int run = hi.w;  // inclusive max-scan of the thread totals
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, run, o);
+        if (lane >= o) run = max(run, y);
+    }
+    if (lane == 31) sh.warp_max[wid] = run;
+    __syncthreads();
+    int pre = __shfl_up_sync(0xffffffffu, run, 1);
+    if (lane == 0) pre = -1;
+    for (int k = 0; k < wid; ++k) pre = max(pre, sh.warp_max[k]);
+    lo = make_int4(max(lo.x, pre), max(lo.y, pre), max(lo.z, pre), max(lo.w, pre));
+    hi = make_int4(max(hi.x, pre), max(hi.y, pre), max(hi.z, pre), max(hi.w, pre));
+    row4[2 * t] = lo;
+    row4[2 * t + 1] = hi;
+    __syncthreads();
+}
+
 // Returns false (for the whole CTA) when the CTA has no edges.
 __device__ __forceinline__ bool edge_chunk(const int32_t *__restrict__ rowptr, int64_t n_rows_used,
-                                           int64_t nnz, const Workspace &ws, int32_t *s_rp,
+                                           int64_t nnz, const Workspace &ws, EdgeRows &sh,
                                            EdgeChunk &c) {
     const int64_t e0 = rowptr[0], e_end = rowptr[n_rows_used];
     if (e0 < 0 || e_end > nnz || e_end < e0) return false;  // flagged during plan
@@ -613,16 +758,17 @@ __device__ __forceinline__ bool edge_chunk(const int32_t *__restrict__ rowptr, i
     }
     c.nr = c.r1 - c.r0 + 1;
     c.staged = c.nr <= kEdgeStage;
-    if (c.staged)
-        for (int64_t i = threadIdx.x; i < c.nr; i += kEdgeThreads) s_rp[i] = rowptr[c.r0 + i];
-    __syncthreads();
+    if (c.staged) {
+        for (int64_t i = threadIdx.x; i < c.nr; i += kEdgeThreads) sh.rp[i] = rowptr[c.r0 + i];
+        edge_rows_build(sh, c);  // its first barrier orders these stores
+    }
     return true;
 }
 
 __device__ __forceinline__ int64_t chunk_row_of(const int32_t *__restrict__ rowptr,
-                                                const int32_t *s_rp, const EdgeChunk &c,
+                                                const EdgeRows &sh, const EdgeChunk &c,
                                                 int64_t e) {
-    return c.staged ? c.r0 + last_le(s_rp, 0, c.nr - 1, e) : last_le(rowptr, c.r0, c.r1, e);
+    return c.staged ? c.r0 + sh.row[e - c.eb] : last_le(rowptr, c.r0, c.r1, e);
 }
 
 // ---- plan, windows above kWarpCap edges: merge ranks ---------------------------
@@ -636,21 +782,21 @@ __device__ __forceinline__ int64_t chunk_row_of(const int32_t *__restrict__ rowp
 // flag go to the merged position; one scan of the flags then gives every
 // merged position its rank among distinct columns (k_merge_emit).  A window
 // with an unsorted row is flagged and redone by the sorting kernels.
-__device__ __forceinline__ int64_t count_lt(const int32_t *a, int64_t n, int32_t x) {
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-        const int64_t m = (lo + hi) >> 1;
-        if (a[m] < x) lo = m + 1; else hi = m;
+// Elements of the sorted a[0, n) below x (LE: at or below x), n < 2^31.
+// Branch-free halving: the answer stays in [base, base + n] and every probe
+// a[base + half] is inside the array.
+template <bool LE>
+__device__ __forceinline__ int count_below(const int32_t *__restrict__ a, int n, int32_t x) {
+    if (n <= 0) return 0;
+    int base = 0;
+    while (n > 1) {
+        const int half = n >> 1;
+        const int32_t v = a[base + half];
+        base = (LE ? v <= x : v < x) ? base + half : base;
+        n -= half;
     }
-    return lo;
-}
-__device__ __forceinline__ int64_t count_le(const int32_t *a, int64_t n, int32_t x) {
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-        const int64_t m = (lo + hi) >> 1;
-        if (a[m] <= x) lo = m + 1; else hi = m;
-    }
-    return lo;
+    const int32_t v = a[base];
+    return base + ((LE ? v <= x : v < x) ? 1 : 0);
 }
 
 // Mark window w as holding an unsorted row and list it once.
@@ -661,17 +807,19 @@ __device__ __forceinline__ void flag_unsorted(const Workspace &ws, int64_t w) {
 __global__ void __launch_bounds__(kEdgeThreads) k_merge_rank(
     const int32_t *__restrict__ rowptr, const int32_t *__restrict__ col, int64_t n_rows_used,
     int window, int64_t nnz, int64_t n_cols, Workspace ws) {
-    __shared__ int32_t s_rp[kEdgeStage];
+    __shared__ EdgeRows sh;
     EdgeChunk c;
-    if (!edge_chunk(rowptr, n_rows_used, nnz, ws, s_rp, c)) return;
+    if (!edge_chunk(rowptr, n_rows_used, nnz, ws, sh, c)) return;
     for (int64_t e = c.eb + threadIdx.x; e < c.ee; e += kEdgeThreads) {
-        const int64_t row = chunk_row_of(rowptr, s_rp, c, e);
-        const int64_t w = row / window, i = row - w * window, wb = w * window;
+        const int64_t row = chunk_row_of(rowptr, sh, c, e);
+        const int64_t w = row / window, wb = w * window;
+        const int i = (int)(row - wb);
         const int64_t b0 = rowptr[wb], b1 = rowptr[wb + window];
         if (b1 - b0 <= kWarpCap) continue;  // k_unique_warp's window (flags stay 0)
         const int32_t x = col[e];
         if (x < 0 || x >= n_cols) atomicOr(ws.flags, FLAG_BAD_COL);
-        const int64_t p = e - rowptr[row];
+        // positions are below 2^31 (int32 rowptr)
+        const int p = (int)(e - rowptr[row]);
         bool first = true;
         if (p > 0) {
             const int32_t prev = col[e - 1];
@@ -681,14 +829,16 @@ __global__ void __launch_bounds__(kEdgeThreads) k_merge_rank(
         int64_t m = p;
         for (int k = 0; k < window; ++k) {
             if (k == i) continue;
-            const int64_t rs = rowptr[wb + k], len = rowptr[wb + k + 1] - rs;
+            const int32_t rs = rowptr[wb + k];
+            const int len = rowptr[wb + k + 1] - rs;
             if (len <= 0) continue;
+            const int32_t *rk = col + rs;
             if (k < i) {
-                const int64_t ub = count_le(col + rs, len, x);
+                const int ub = count_below<true>(rk, len, x);
                 m += ub;
-                if (ub > 0 && col[rs + ub - 1] == x) first = false;
+                if (ub > 0 && rk[ub - 1] == x) first = false;
             } else {
-                m += count_lt(col + rs, len, x);
+                m += count_below<false>(rk, len, x);
             }
         }
         if (m < 0 || m >= b1 - b0) {  // only when a row is unsorted
@@ -706,11 +856,11 @@ __global__ void __launch_bounds__(kEdgeThreads) k_merge_rank(
 __global__ void __launch_bounds__(kEdgeThreads) k_merge_emit(
     const int32_t *__restrict__ rowptr, int64_t n_rows_used, int window, int64_t nnz,
     Workspace ws) {
-    __shared__ int32_t s_rp[kEdgeStage];
+    __shared__ EdgeRows sh;
     EdgeChunk c;
-    if (!edge_chunk(rowptr, n_rows_used, nnz, ws, s_rp, c)) return;
+    if (!edge_chunk(rowptr, n_rows_used, nnz, ws, sh, c)) return;
     for (int64_t e = c.eb + threadIdx.x; e < c.ee; e += kEdgeThreads) {
-        const int64_t row = chunk_row_of(rowptr, s_rp, c, e);
+        const int64_t row = chunk_row_of(rowptr, sh, c, e);
         const int64_t w = row / window, wb = w * window;
         const int64_t b0 = rowptr[wb], b1 = rowptr[wb + window];
         if (b1 - b0 <= kWarpCap || ws.wflag[w]) continue;
@@ -962,11 +1112,11 @@ __global__ void __launch_bounds__(kEdgeThreads) k_fill_edges(
     const void *__restrict__ deg, int deg_dtype, VT *__restrict__ out_val,
     int32_t *__restrict__ out_map, int32_t *__restrict__ out_map_t,
     int32_t *__restrict__ out_edge_slot, int64_t nnz, int64_t n_slots) {
-    __shared__ int32_t s_rp[kEdgeStage];
+    __shared__ EdgeRows sh;
     EdgeChunk c;
-    if (!edge_chunk(rowptr, n_rows_used, nnz, ws, s_rp, c)) return;
+    if (!edge_chunk(rowptr, n_rows_used, nnz, ws, sh, c)) return;
     for (int64_t e = c.eb + threadIdx.x; e < c.ee; e += kEdgeThreads)
-        fill_edge<VT>(e, chunk_row_of(rowptr, s_rp, c, e), rowptr, col, window, wide, n_cols,
+        fill_edge<VT>(e, chunk_row_of(rowptr, sh, c, e), rowptr, col, window, wide, n_cols,
                       n_rows, ws, deg, deg_dtype, out_val, out_map, out_map_t, out_edge_slot,
                       n_slots);
 }
@@ -985,7 +1135,8 @@ template <typename KT, int CAP, int LO>
 int launch_unique_warp(unsigned grid, const int32_t *rowptr, const int32_t *col, int64_t nw,
                        int window, int64_t nnz, int64_t n_cols, int unsorted_only, Workspace ws,
                        cudaStream_t st) {
-    constexpr size_t smem = (size_t)kWarpSortWarps * CAP * sizeof(KT);
+    // register sort up to kWarpCap edges: no shared memory
+    constexpr size_t smem = CAP == kWarpCap ? 0 : (size_t)kWarpSortWarps * CAP * sizeof(KT);
     auto kernel = k_unique_warp<KT, CAP, LO>;
     if (smem > 48 * 1024) {
         static std::once_flag once;
