@@ -124,10 +124,16 @@ __device__ __forceinline__ void mma_1688_tf32(float (&d)[4], uint32_t a0, uint32
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ uint32_t f32_to_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
-    return r;
+// fp32 -> (hi, lo) operands of a 3xTF32 product (hi*hi + hi*lo + lo*hi), the
+// split of Ootomo and Yokota (2022, "Recovering single precision accuracy
+// from Tensor Cores while surpassing the FP32 theoretical peak performance")
+// with truncation: hi keeps the sign, exponent and top 10 mantissa bits of x,
+// lo is the remainder x - hi (exact in fp32) truncated the same way, so
+// |x - hi - lo| < 2^-20 |x|.  Two logic operations and one add, all
+// full-rate, instead of two conversions.
+__device__ __forceinline__ void split_tf32x3(float x, uint32_t &hi, uint32_t &lo) {
+    hi = __float_as_uint(x) & 0xffffe000u;
+    lo = __float_as_uint(x - __uint_as_float(hi)) & 0xffffe000u;
 }
 
 __device__ __forceinline__ void red_add_f32(float *p, float v) {

@@ -411,10 +411,6 @@ __global__ void __launch_bounds__(kSThreads) k_sddmm16(SddmmArgs P) {
 }
 
 // fp32 operands, 3xTF32: S[col][row] with m16n8k8
-__device__ __forceinline__ void split_tf32s(float x, uint32_t &hi, uint32_t &lo) {
-    hi = f32_to_tf32(x);
-    lo = f32_to_tf32(x - __uint_as_float(hi));
-}
 
 // the fp32 kernel also keeps each warp's window rows (W x FC, rows padded by
 // 4 floats against bank conflicts) in shared memory, after the stage ring
@@ -514,14 +510,14 @@ __global__ void __launch_bounds__(kSThreads) k_sddmm_tf32(SddmmArgs P) {
                     const int m = gid + 8 * (u & 1);
                     const int f = 8 * kk + tig + 4 * (u >> 1);
                     const float x = xsg[m * FC + (((f >> 2) ^ (m & 7)) << 2) + (f & 3)];
-                    split_tf32s(x, ah[u], al[u]);
+                    split_tf32x3(x, ah[u], al[u]);
                 }
 #pragma unroll
                 for (int t = 0; t < C::NT; ++t) {
                     uint32_t bh[2], bl[2];
                     const float *qr = qs + (t * 8 + gid) * Q::QROW + 8 * kk + tig;
-                    split_tf32s(qr[0], bh[0], bl[0]);
-                    split_tf32s(qr[4], bh[1], bl[1]);
+                    split_tf32x3(qr[0], bh[0], bl[0]);
+                    split_tf32x3(qr[4], bh[1], bl[1]);
                     mma_1688_tf32(acc[t], al[0], al[1], al[2], al[3], bh[0], bh[1]);
                     mma_1688_tf32(acc[t], ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
                     mma_1688_tf32(acc[t], ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);

@@ -121,10 +121,6 @@ __device__ __forceinline__ int swz_rb(int r) {
     else return (r >> 1) & 3;
 }
 
-__device__ __forceinline__ void split_tf32f(float x, uint32_t &hi, uint32_t &lo) {
-    hi = f32_to_tf32(x);
-    lo = f32_to_tf32(x - __uint_as_float(hi));
-}
 
 // PSPLIT: aggregate with P as a hi + lo pair of 16-bit values (fp32-accurate
 // output); the training path needs it so that dout . out matches the
@@ -339,9 +335,9 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                         ldsm_x4(xs + mrow * C::XROW + ((ch ^ swz_rb<C::XROW>(mrow)) << 4), a[0], a[1],
                                 a[2], a[3]);
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) split_tf32f(__uint_as_float(a[u]), ah[u], al[u]);
-                        split_tf32f(bqf[kk][0], bh[0], bl[0]);
-                        split_tf32f(bqf[kk][1], bh[1], bl[1]);
+                        for (int u = 0; u < 4; ++u) split_tf32x3(__uint_as_float(a[u]), ah[u], al[u]);
+                        split_tf32x3(bqf[kk][0], bh[0], bl[0]);
+                        split_tf32x3(bqf[kk][1], bh[1], bl[1]);
                         mma_1688_tf32(sv, al[0], al[1], al[2], al[3], bh[0], bh[1]);
                         mma_1688_tf32(sv, ah[0], ah[1], ah[2], ah[3], bl[0], bl[1]);
                         mma_1688_tf32(sv, ah[0], ah[1], ah[2], ah[3], bh[0], bh[1]);
@@ -432,8 +428,8 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                     uint32_t ph[2][2], pl[2][2];
 #pragma unroll
                     for (int ks = 0; ks < 2; ++ks) {
-                        split_tf32f(ptile[(8 * ks + tig) * kW + gid], ph[ks][0], pl[ks][0]);
-                        split_tf32f(ptile[(8 * ks + tig + 4) * kW + gid], ph[ks][1], pl[ks][1]);
+                        split_tf32x3(ptile[(8 * ks + tig) * kW + gid], ph[ks][0], pl[ks][0]);
+                        split_tf32x3(ptile[(8 * ks + tig + 4) * kW + gid], ph[ks][1], pl[ks][1]);
                     }
                     const float *xt = (const float *)(sgen + cstage * C::STAGE);
 #pragma unroll
@@ -447,7 +443,7 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                                 const int c = 8 * ks + tig + 4 * (u >> 1);
                                 const int f = 16 * j + gid + 8 * (u & 1);
                                 const float x = xt[c * F + (((f >> 2) ^ swz_rb<C::XROW>(c)) << 2) + (f & 3)];
-                                split_tf32f(x, ah[u], al[u]);
+                                split_tf32x3(x, ah[u], al[u]);
                             }
                             mma_1688_tf32(acc[j], al[0], al[1], al[2], al[3], ph[ks][0], ph[ks][1]);
                             mma_1688_tf32(acc[j], ah[0], ah[1], ah[2], ah[3], pl[ks][0], pl[ks][1]);

@@ -261,8 +261,9 @@ __global__ void __launch_bounds__(kThreads, (Cfg16<T, W, FC, WIDE, S>::MINB)) k_
                     const IT f = fa + (h >> 1) * 8;
                     if (r < m_out && (full || f < F)) {
                         float *dst = Y + (r * ldy + f);
+                        // Y is written once: a streaming store leaves L2 to the X rows
                         if (add) red_add_f32(dst, acc[j][t][h]);
-                        else *dst = acc[j][t][h];
+                        else __stcs(dst, acc[j][t][h]);
                     }
                     acc[j][t][h] = 0.f;
                 }
@@ -697,10 +698,6 @@ struct CfgTF32 {
     static constexpr int VCH = VSTAGE / 16;
 };
 
-__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
-    hi = f32_to_tf32(x);
-    lo = f32_to_tf32(x - __uint_as_float(hi));
-}
 
 template <int W, int FC, int WIDE, int S>
 __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
@@ -812,7 +809,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
                         const int c = 8 * h + tig + 4 * u;
                         const int r = t * 8 + gid;
                         const float v = vsg[(c / WIDE) * W * WIDE + r * WIDE + c % WIDE];
-                        split_tf32(v, bh[t][u], bl[t][u]);
+                        split_tf32x3(v, bh[t][u], bl[t][u]);
                     }
                 }
 #pragma unroll
@@ -824,7 +821,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_tf32(
                         const int f = 16 * j + gid + ((u & 1) << 3);
                         const int ch = f >> 2;
                         const float x = xsg[k * FC + (((ch ^ ((k & 3) << 1))) << 2) + (f & 3)];
-                        split_tf32(x, ah[u], al[u]);
+                        split_tf32x3(x, ah[u], al[u]);
                     }
 #pragma unroll
                     for (int t = 0; t < C::NT; ++t) {

@@ -344,8 +344,10 @@ def test_autotune_spmm_picks_a_measured_shape(cuda, restore_spmm_options, dtype)
     """tune_spmm times every candidate shape and returns the fastest without
     changing the options in effect afterwards (read back through
     att_get_option); the chosen shape, passed per call, gives the default
-    shape's result (same arithmetic; atomics may reorder fp32 adds), and the
-    next call without a shape is back at the defaults."""
+    shape's result (same arithmetic; atomics may reorder fp32 adds -- except
+    FP8, whose two kernels round the scaled products in different places and
+    agree within 2e-3), and the next call without a shape is back at the
+    defaults."""
     from att_gb300 import _lib, autotune, graphs, ops
     import ctypes
     rowptr, col = graphs.random_csr(2000, 2000, 25, seed=9, hub_rows=3, hub_len=1500)
@@ -377,7 +379,8 @@ def test_autotune_spmm_picks_a_measured_shape(cuda, restore_spmm_options, dtype)
     assert options() == before
     Y1 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale,
                   shape=choice)
-    assert oracle.rel_err(Y1.cpu().numpy(), Y0.cpu().numpy()) <= 1e-6
+    same = 2e-3 if dtype == torch.float8_e4m3fn else 1e-6
+    assert oracle.rel_err(Y1.cpu().numpy(), Y0.cpu().numpy()) <= same
     # a call without a shape runs (and leaves the thread) at the defaults
     Y2 = ops.spmm(f.rowptr, f.col, val, f.window_of_part, f.atomic, Xk, 2000, x_scale=scale)
     assert options() == before
