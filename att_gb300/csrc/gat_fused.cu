@@ -139,6 +139,8 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
     const IT H = (IT)A.H, n_nodes = (IT)A.n_nodes, ldx = (IT)A.ldx, ldo = (IT)A.ldo;
     const T *X = (const T *)A.X;
     const float NEG_INF = -INFINITY;
+    // logits may exceed a row's reference by this much before it moves
+    constexpr float kLazy = 8.f;
     float *ptile = (float *)(smem + warp * C::WARP_SMEM + kGStages * C::STAGE);  // fp32 only
     (void)ptile;
 
@@ -359,35 +361,31 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                     const float x = sv[u];
                     sv[u] = occ ? (x > 0.f ? x : A.slope * x) : NEG_INF;
                 }
-                // online softmax, rows 2tig (u even) and 2tig+1 (u odd)
-                float mx[2] = {fmaxf(sv[0], sv[2]), fmaxf(sv[1], sv[3])};
+                // online softmax, rows 2tig (u even) and 2tig+1 (u odd), with
+                // lazy rescaling: a row's reference m_run moves (max over the
+                // row's lanes, accumulators and partial sums rescaled) only on
+                // its first occupied slot or when a logit exceeds it by more
+                // than kLazy, so most steps run no reduction at all; the
+                // probabilities stay below e^kLazy, well inside the 16-bit P
+                // range.  Each lane sums its own columns' probabilities
+                // (l_run holds that partial until the end of the item).
+                const bool up = sv[0] > m_run[0] + kLazy || sv[2] > m_run[0] + kLazy ||
+                                sv[1] > m_run[1] + kLazy || sv[3] > m_run[1] + kLazy;
+                if (__any_sync(0xffffffffu, up)) {
+                    float mx[2] = {fmaxf(sv[0], sv[2]), fmaxf(sv[1], sv[3])};
 #pragma unroll
-                for (int o = 4; o < 32; o <<= 1) {
-                    mx[0] = fmaxf(mx[0], __shfl_xor_sync(0xffffffffu, mx[0], o));
-                    mx[1] = fmaxf(mx[1], __shfl_xor_sync(0xffffffffu, mx[1], o));
-                }
-                float alpha[2], mref[2];
+                    for (int o = 4; o < 32; o <<= 1) {
+                        mx[0] = fmaxf(mx[0], __shfl_xor_sync(0xffffffffu, mx[0], o));
+                        mx[1] = fmaxf(mx[1], __shfl_xor_sync(0xffffffffu, mx[1], o));
+                    }
+                    float alpha[2];
 #pragma unroll
-                for (int u = 0; u < 2; ++u) {
-                    const float mn = fmaxf(m_run[u], mx[u]);
-                    mref[u] = mn == NEG_INF ? 0.f : mn;
-                    alpha[u] = __expf(m_run[u] - mref[u]);
-                    m_run[u] = mn;
-                }
-                float p[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) p[u] = __expf(sv[u] - mref[u & 1]);
-                float ps[2] = {p[0] + p[2], p[1] + p[3]};
-#pragma unroll
-                for (int o = 4; o < 32; o <<= 1) {
-                    ps[0] += __shfl_xor_sync(0xffffffffu, ps[0], o);
-                    ps[1] += __shfl_xor_sync(0xffffffffu, ps[1], o);
-                }
-                l_run[0] = l_run[0] * alpha[0] + ps[0];
-                l_run[1] = l_run[1] * alpha[1] + ps[1];
-                // rescale only when some row's max moved (rare after a window's
-                // first steps); alpha is exactly 1 otherwise
-                if (__any_sync(0xffffffffu, alpha[0] != 1.f || alpha[1] != 1.f)) {
+                    for (int u = 0; u < 2; ++u) {
+                        const float mn = fmaxf(m_run[u], mx[u]);
+                        alpha[u] = mn == NEG_INF ? 1.f : __expf(m_run[u] - mn);
+                        l_run[u] *= alpha[u];
+                        m_run[u] = mn;
+                    }
 #pragma unroll
                     for (int j = 0; j < C::MT; ++j) {
                         acc[j][0] *= alpha[0];
@@ -396,6 +394,13 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                         acc[j][3] *= alpha[1];
                     }
                 }
+                const float mref[2] = {m_run[0] == NEG_INF ? 0.f : m_run[0],
+                                       m_run[1] == NEG_INF ? 0.f : m_run[1]};
+                float p[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) p[u] = __expf(sv[u] - mref[u & 1]);
+                l_run[0] += p[0] + p[2];
+                l_run[1] += p[1] + p[3];
                 if constexpr (!C::F32) {
                     // P^T into B fragments: (col gid, rows 2tig..) -> (row gid, cols 2tig..)
                     const uint32_t h01 = pack2<T>(p[0], p[1]), h23 = pack2<T>(p[2], p[3]);
@@ -460,6 +465,12 @@ __global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
                 cstage = cstage + 1 == kGStages ? 0 : cstage + 1;
                 pstage = pstage + 1 == kGStages ? 0 : pstage + 1;
             }
+        }
+        // row sums: the lanes' partial sums over their own columns
+#pragma unroll
+        for (int o = 4; o < 32; o <<= 1) {
+            l_run[0] += __shfl_xor_sync(0xffffffffu, l_run[0], o);
+            l_run[1] += __shfl_xor_sync(0xffffffffu, l_run[1], o);
         }
         // ---- epilogue: acc[j] = (feature 16j+gid (+8), rows 2tig, 2tig+1) ----
         const int slot = A.chunk_slot[chunk];
@@ -866,15 +877,10 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
                 p[u] = pv;
                 dz[u] = pv * (dp[u] - cc) * (z > 0.f ? 1.f : A.slope);
             }
-            // ds1 (rows): sum over the 16 columns
-            float r0 = dz[0] + dz[2], r1 = dz[1] + dz[3];
-#pragma unroll
-            for (int o = 4; o < 32; o <<= 1) {
-                r0 += __shfl_xor_sync(0xffffffffu, r0, o);
-                r1 += __shfl_xor_sync(0xffffffffu, r1, o);
-            }
-            ds1_acc[0] += r0;
-            ds1_acc[1] += r1;
+            // ds1 (rows): each lane sums its own columns; the row's lanes are
+            // reduced once per work item
+            ds1_acc[0] += dz[0] + dz[2];
+            ds1_acc[1] += dz[1] + dz[3];
             // ds0 (columns): sum over the 8 rows, one atomic per column
             float c_lo = dz[0] + dz[1], c_hi = dz[2] + dz[3];
 #pragma unroll
@@ -924,6 +930,11 @@ __global__ void __launch_bounds__(kGThreads) k_gat_backward(GatBwdArgs A) {
                 const int f = 16 * j + gid + 8 * (u >> 1);
                 if (row < n_nodes) red_add_f32(A.dXp + row * ldg + h * F + f, acc[j][u]);
             }
+#pragma unroll
+        for (int o = 4; o < 32; o <<= 1) {
+            ds1_acc[0] += __shfl_xor_sync(0xffffffffu, ds1_acc[0], o);
+            ds1_acc[1] += __shfl_xor_sync(0xffffffffu, ds1_acc[1], o);
+        }
         if (gid == 0) {
 #pragma unroll
             for (int u = 0; u < 2; ++u) {

@@ -449,7 +449,7 @@ class Server:
 
     def __init__(self, model, budget=120e9, max_active=64, workers=2, use_graph=True,
                  keep_outputs=True, max_inflight_ticks=2, group_parts=GROUP_PARTS,
-                 direct_output=True, checksum=False):
+                 direct_output=False, checksum=False, idle_sleep=2e-5):
         require_cuda()
         self.model = model
         self.adm = Admission(budget, max_active)
@@ -467,10 +467,18 @@ class Server:
         self.batched = BatchedSpmm(max_active, use_graph=use_graph)
         self.keep_outputs = keep_outputs
         self.max_inflight = max_inflight_ticks
-        # layer 2 writes its fp32 result straight into pinned host memory over
-        # the coherent CPU-GPU link (no device buffer, no separate copy)
+        # direct_output: layer 2 writes its fp32 result straight into pinned
+        # host memory over the CPU-GPU link (no device buffer, no separate
+        # copy).  Off by default: the kernel's scattered 32-byte stores cross
+        # the link slowly (the 2.45M-node SpMM takes 14.4 ms that way against
+        # 2.18 ms into HBM), and on the 32-graph Poisson trace it gave a higher
+        # p99 on every seed than a device result copied out on the copy stream
         self.direct_output = direct_output
         self.checksum = checksum
+        # seconds the loop sleeps when nothing advanced (0: yield the core
+        # and poll again); 0 and 20 us measured the same p50 / p99 on the
+        # 32-graph Poisson trace
+        self.idle_sleep = idle_sleep
         self.jobs_per_tick = []
 
     def _finish(self, r, now, est):
@@ -652,7 +660,7 @@ class Server:
                     still.append(r)
             drains = still
             if not busy:
-                time.sleep(2e-5)
+                time.sleep(self.idle_sleep)
         torch.cuda.synchronize()
         self.batched.check()
         return requests
