@@ -37,6 +37,11 @@ _SIGNATURES = {
     "att_block_fill": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int, _c_int,
                                 _c_int, _c_vp, _c_int, _c_vp, _c_sz, _c_vp, _c_vp, _c_vp, _c_int,
                                 _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "att_block_fill_async": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int,
+                                      _c_int, _c_int, _c_vp, _c_int, _c_vp, _c_sz, _c_i64,
+                                      _c_i64, _c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,
+                                      _c_vp, _c_vp, _c_vp, _c_vp]),
+    "att_block_fill_result": (_c_int, [_c_vp, _c_int]),
     "att_block_convert_noalloc_max_scratch": (_c_sz, []),
     "att_block_convert_noalloc": (_c_int, [_c_vp, _c_vp, _c_i64, _c_i64, _c_i64, _c_int, _c_int,
                                            _c_int, _c_int, _c_vp, _c_int, _c_vp, _c_vp, _c_vp,

@@ -1320,14 +1320,12 @@ extern "C" int att_block_plan_result(const int64_t *summary, int64_t n_cols, int
     return plan_check(summary, window, n_cols, n_parts_out, n_condensed_out);
 }
 
-extern "C" int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
-                              int64_t nnz, int64_t n_cols, int window, int wide, int part,
-                              int emit_empty, const void *deg, int deg_dtype,
-                              const void *workspace, size_t workspace_bytes, int32_t *out_rowptr,
-                              int32_t *out_col, void *out_val, int val_dtype, int32_t *out_map,
-                              int32_t *out_map_t, int32_t *out_edge_slot, int32_t *out_window,
-                              int32_t *out_atomic, void *stream) {
-    clear_error();
+namespace {
+// Argument checks shared by the fill entry points; lays out `ws`.
+int fill_checks(const int32_t *rowptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                int64_t n_cols, int window, int wide, int part, const void *deg, int deg_dtype,
+                const void *workspace, size_t workspace_bytes, int32_t *out_rowptr,
+                const void *out_val, int val_dtype, Workspace &ws) {
     int s = check_conv_args(rowptr, col, n_rows, nnz, n_cols, window, wide, part);
     if (s != ATT_OK) return s;
     size_t need = workspace_layout(n_rows, nnz, n_cols, window, nullptr, nullptr);
@@ -1340,15 +1338,21 @@ extern "C" int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t
         ATT_CHECK(val_dtype == ATT_F16 || val_dtype == ATT_BF16 || val_dtype == ATT_F32,
                   ATT_ERR_INVALID, "val_dtype must be f16, bf16 or f32");
     }
-    Workspace ws;
     workspace_layout(n_rows, nnz, n_cols, window, &ws, (char *)workspace);
-    cudaStream_t st = (cudaStream_t)stream;
+    return ATT_OK;
+}
+
+
+// Enqueue the fill of a plan with n_cond condensed columns and n_parts parts
+// (the plan's own sizes) on `st`; no synchronisation.
+int fill_enqueue(const int32_t *rowptr, const int32_t *col, int64_t n_rows, int64_t nnz,
+                 int64_t n_cols, int window, int wide, int part, const void *deg, int deg_dtype,
+                 const Workspace &ws, int64_t n_cond, int64_t n_parts, int32_t *out_rowptr,
+                 int32_t *out_col, void *out_val, int val_dtype, int32_t *out_map,
+                 int32_t *out_map_t, int32_t *out_edge_slot, int32_t *out_window,
+                 int32_t *out_atomic, cudaStream_t st) {
+    int s = ATT_OK;
     const int64_t nw = n_windows(n_rows, window);
-    int64_t tot[2] = {0, 0};
-    ATT_CUDA(cudaMemcpyAsync(&tot[0], ws.col_off + nw, 8, cudaMemcpyDeviceToHost, st), "d2h");
-    ATT_CUDA(cudaMemcpyAsync(&tot[1], ws.part_off + nw, 8, cudaMemcpyDeviceToHost, st), "d2h");
-    ATT_CUDA(cudaStreamSynchronize(st), "fill sync");
-    const int64_t n_cond = tot[0], n_parts = tot[1];
     ATT_CHECK(n_cond == 0 || out_col != nullptr, ATT_ERR_INVALID, "col output is null");
     ATT_CHECK(n_parts == 0 || (out_window && out_atomic), ATT_ERR_INVALID,
               "window/atomic output is null");
@@ -1401,12 +1405,77 @@ extern "C" int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t
         s = launch_status("k_fill_edges");
         if (s != ATT_OK) return s;
     }
-    int32_t flags[4];
-    ATT_CUDA(cudaMemcpyAsync(flags, ws.flags, 16, cudaMemcpyDeviceToHost, st), "d2h");
-    ATT_CUDA(cudaStreamSynchronize(st), "fill sync");
-    ATT_CHECK(!(out_map_t && (flags[0] & FLAG_UNSORTED)), ATT_ERR_FORMAT,
+    return ATT_OK;
+}
+
+// Status of a fill from its device-side flags.
+int fill_flags_status(const int32_t *flags, int want_map_t) {
+    ATT_CHECK(!(want_map_t && (flags[0] & FLAG_UNSORTED)), ATT_ERR_FORMAT,
               "mirrored-edge map needs every CSR row sorted by column");
     ATT_CHECK(!(flags[0] & FLAG_OVERFLOW), ATT_ERR_FORMAT,
               "the workspace does not hold a plan of this CSR (run att_block_plan first)");
     return ATT_OK;
+}
+}  // namespace
+
+extern "C" int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
+                              int64_t nnz, int64_t n_cols, int window, int wide, int part,
+                              int emit_empty, const void *deg, int deg_dtype,
+                              const void *workspace, size_t workspace_bytes, int32_t *out_rowptr,
+                              int32_t *out_col, void *out_val, int val_dtype, int32_t *out_map,
+                              int32_t *out_map_t, int32_t *out_edge_slot, int32_t *out_window,
+                              int32_t *out_atomic, void *stream) {
+    clear_error();
+    (void)emit_empty;  // the plan decided the parts
+    Workspace ws;
+    int s = fill_checks(rowptr, col, n_rows, nnz, n_cols, window, wide, part, deg, deg_dtype,
+                        workspace, workspace_bytes, out_rowptr, out_val, val_dtype, ws);
+    if (s != ATT_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t nw = n_windows(n_rows, window);
+    int64_t tot[2] = {0, 0};
+    ATT_CUDA(cudaMemcpyAsync(&tot[0], ws.col_off + nw, 8, cudaMemcpyDeviceToHost, st), "d2h");
+    ATT_CUDA(cudaMemcpyAsync(&tot[1], ws.part_off + nw, 8, cudaMemcpyDeviceToHost, st), "d2h");
+    ATT_CUDA(cudaStreamSynchronize(st), "fill sync");
+    const int64_t n_cond = tot[0], n_parts = tot[1];
+    s = fill_enqueue(rowptr, col, n_rows, nnz, n_cols, window, wide, part, deg, deg_dtype, ws,
+                     n_cond, n_parts, out_rowptr, out_col, out_val, val_dtype, out_map, out_map_t,
+                     out_edge_slot, out_window, out_atomic, st);
+    if (s != ATT_OK) return s;
+    int32_t flags[4];
+    ATT_CUDA(cudaMemcpyAsync(flags, ws.flags, 16, cudaMemcpyDeviceToHost, st), "d2h");
+    ATT_CUDA(cudaStreamSynchronize(st), "fill sync");
+    return fill_flags_status(flags, out_map_t != nullptr);
+}
+
+extern "C" int att_block_fill_async(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
+                                    int64_t nnz, int64_t n_cols, int window, int wide, int part,
+                                    int emit_empty, const void *deg, int deg_dtype,
+                                    const void *workspace, size_t workspace_bytes,
+                                    int64_t n_parts, int64_t n_condensed, int32_t *out_rowptr,
+                                    int32_t *out_col, void *out_val, int val_dtype,
+                                    int32_t *out_map, int32_t *out_map_t, int32_t *out_edge_slot,
+                                    int32_t *out_window, int32_t *out_atomic, int32_t *flags,
+                                    void *stream) {
+    clear_error();
+    (void)emit_empty;
+    ATT_CHECK(flags != nullptr && n_parts >= 0 && n_condensed >= 0, ATT_ERR_INVALID,
+              "null flags or negative sizes");
+    Workspace ws;
+    int s = fill_checks(rowptr, col, n_rows, nnz, n_cols, window, wide, part, deg, deg_dtype,
+                        workspace, workspace_bytes, out_rowptr, out_val, val_dtype, ws);
+    if (s != ATT_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    s = fill_enqueue(rowptr, col, n_rows, nnz, n_cols, window, wide, part, deg, deg_dtype, ws,
+                     n_condensed, n_parts, out_rowptr, out_col, out_val, val_dtype, out_map,
+                     out_map_t, out_edge_slot, out_window, out_atomic, st);
+    if (s != ATT_OK) return s;
+    ATT_CUDA(cudaMemcpyAsync(flags, ws.flags, 16, cudaMemcpyDeviceToHost, st), "d2h flags");
+    return ATT_OK;
+}
+
+extern "C" int att_block_fill_result(const int32_t *flags, int with_map_t) {
+    clear_error();
+    ATT_CHECK(flags != nullptr, ATT_ERR_INVALID, "null flags");
+    return fill_flags_status(flags, with_map_t);
 }

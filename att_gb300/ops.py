@@ -104,7 +104,9 @@ def _conv_args(rowptr, col, deg, window, wide, part, emit_empty, val_dtype, want
                 deg_kind=deg_kind, val_dtype=val_dtype)
 
 
-def _conv_fill(a, ws, ws_bytes, P, NC, want_map, want_trans, want_edge_slot):
+def _conv_fill(a, ws, ws_bytes, P, NC, want_map, want_trans, want_edge_slot, flags=None):
+    """att_block_fill, or with ``flags`` (pinned int32 [4]) att_block_fill_async:
+    no host synchronisation, the device-side checks copied to ``flags``."""
     dev = a["rowptr"].device
     W = a["window"]
     out_rowptr = torch.empty(2 * P + 1, dtype=torch.int32, device=dev)
@@ -117,11 +119,18 @@ def _conv_fill(a, ws, ws_bytes, P, NC, want_map, want_trans, want_edge_slot):
     mp = torch.empty(NC * W, dtype=torch.int32, device=dev) if want_map else None
     mpt = torch.empty(NC * W, dtype=torch.int32, device=dev) if want_trans else None
     es = torch.empty(a["nnz"], dtype=torch.int32, device=dev) if want_edge_slot else None
-    _lib.call("att_block_fill", _p(a["rowptr"]), _p(a["col"]), a["n_rows"], a["nnz"],
-              a["n_cols"], W, a["wide"], a["part"], a["emit_empty"], _p(a["deg"]),
-              a["deg_kind"], _p(ws), ws_bytes, _p(out_rowptr), _p(out_col), _p(val),
-              _DT[a["val_dtype"]] if val is not None else _lib.NONE, _p(mp), _p(mpt), _p(es),
-              _p(out_win), _p(out_atomic), _stream())
+    vdt = _DT[a["val_dtype"]] if val is not None else _lib.NONE
+    if flags is None:
+        _lib.call("att_block_fill", _p(a["rowptr"]), _p(a["col"]), a["n_rows"], a["nnz"],
+                  a["n_cols"], W, a["wide"], a["part"], a["emit_empty"], _p(a["deg"]),
+                  a["deg_kind"], _p(ws), ws_bytes, _p(out_rowptr), _p(out_col), _p(val), vdt,
+                  _p(mp), _p(mpt), _p(es), _p(out_win), _p(out_atomic), _stream())
+    else:
+        _lib.call("att_block_fill_async", _p(a["rowptr"]), _p(a["col"]), a["n_rows"], a["nnz"],
+                  a["n_cols"], W, a["wide"], a["part"], a["emit_empty"], _p(a["deg"]),
+                  a["deg_kind"], _p(ws), ws_bytes, P, NC, _p(out_rowptr), _p(out_col), _p(val),
+                  vdt, _p(mp), _p(mpt), _p(es), _p(out_win), _p(out_atomic), _p(flags),
+                  _stream())
     return BlockFormat(rowptr=out_rowptr, col=out_col, window_of_part=out_win, atomic=out_atomic,
                        window=W, wide=a["wide"], part=a["part"], n_rows=a["n_rows"],
                        n_cols=a["n_cols"], nnz=a["nnz"], val=val, map=mp, map_t=mpt,
@@ -184,10 +193,14 @@ def block_convert_async(rowptr, col, deg=None, window=8, wide=8, part=32, emit_e
     return PendingConvert(a, ws, ws_bytes, summary, ev, (want_map, want_trans, want_edge_slot))
 
 
-def block_convert_finish(pending):
+def block_convert_finish(pending, check_later=False):
     """Phase 2: validate the plan's summary (raises AttError for a malformed
     CSR) and enqueue the fill on the current stream (the plan's stream, or one
-    ordered after it)."""
+    ordered after it).  The fill's device-side checks are read back with a
+    host synchronisation -- or, with ``check_later``, copied to pinned memory
+    without one: the format then carries them (``fmt.extra["fill_flags"]``,
+    with the workspace the fill reads) and ``block_fill_check(fmt)`` raises
+    their error once the stream has passed the fill."""
     if not pending.event.query():
         raise RuntimeError("the plan has not completed: wait for pending.ready()")
     n_parts = _lib.ctypes.c_int64(0)
@@ -195,8 +208,22 @@ def block_convert_finish(pending):
     a = pending.args
     _lib.call("att_block_plan_result", _p(pending.summary), a["n_cols"], a["window"],
               _lib.ctypes.byref(n_parts), _lib.ctypes.byref(n_cond))
-    return _conv_fill(a, pending.ws, pending.ws_bytes, n_parts.value, n_cond.value,
-                      *pending.options)
+    flags = torch.zeros(4, dtype=torch.int32).pin_memory() if check_later else None
+    fmt = _conv_fill(a, pending.ws, pending.ws_bytes, n_parts.value, n_cond.value,
+                     *pending.options, flags=flags)
+    if flags is not None:
+        fmt.extra["fill_flags"] = flags
+        fmt.extra["fill_workspace"] = pending.ws  # read by the fill until the stream passes it
+    return fmt
+
+
+def block_fill_check(fmt):
+    """Raise the error of a fill enqueued with ``check_later`` (call once the
+    stream has passed it)."""
+    flags = fmt.extra.pop("fill_flags", None)
+    if flags is not None:
+        fmt.extra.pop("fill_workspace", None)
+        _lib.call("att_block_fill_result", _p(flags), 1 if fmt.map_t is not None else 0)
 
 
 _SHAPE_KNOBS = {"spmm": ("spmm_fc", "spmm_stages"), "fp8": ("spmm_fp8",),

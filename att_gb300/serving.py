@@ -515,7 +515,8 @@ class Server:
         model = self.model
         s = self.streams[r.dev["sidx"]]
         with torch.cuda.stream(s):
-            fmt = ops.block_convert_finish(r.dev.pop("pending"))
+            # the fill's checks come back with the groups' counts: no host wait
+            fmt = ops.block_convert_finish(r.dev.pop("pending"), check_later=True)
             pg = spmm_groups_async(fmt, self.group_parts, m_out=r.n)
         r.dev.update({"fmt": fmt, "pgroups": pg})
         r.event = pg.event
@@ -523,6 +524,7 @@ class Server:
     def _ready(self, r):
         model = self.model
         s = self.streams[r.dev["sidx"]]
+        ops.block_fill_check(r.dev["fmt"])  # the stream has passed the fill (groups after it)
         g = r.dev.pop("pgroups").finish()
         F = max(model.hidden, model.F_out)
         with torch.cuda.stream(s):
@@ -597,7 +599,11 @@ class Server:
                     still.append(r)
                     continue
                 busy = True
-                self._ready(r)
+                try:
+                    self._ready(r)
+                except Exception as e:  # a check of the fill failed
+                    fail(r, e)
+                    continue
                 free_streams.append(r.dev["sidx"])
                 r.stage = 2
                 ready1.append(r)

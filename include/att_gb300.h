@@ -145,6 +145,22 @@ ATT_API int att_block_fill(const int32_t *rowptr, const int32_t *col, int64_t n_
                    int32_t *out_map, int32_t *out_map_t, int32_t *out_edge_slot,
                    int32_t *out_window, int32_t *out_atomic, void *stream);
 
+/* Phase 2 without the synchronisations (no counterpart in the reference):
+ * the sizes come from att_block_plan_result of the same plan, and the
+ * device-side checks go to `flags` (4 int32, pinned host memory for an
+ * asynchronous copy).  Once `stream` has passed that copy,
+ * att_block_fill_result(flags, map_t != NULL) returns what att_block_fill
+ * would have returned.  For a scheduler that must not block (the serving
+ * loop). */
+ATT_API int att_block_fill_async(const int32_t *rowptr, const int32_t *col, int64_t n_rows,
+                   int64_t nnz, int64_t n_cols, int window, int wide, int part, int emit_empty,
+                   const void *deg, int deg_dtype, const void *workspace, size_t workspace_bytes,
+                   int64_t n_parts, int64_t n_condensed, int32_t *out_rowptr, int32_t *out_col,
+                   void *out_val, int val_dtype, int32_t *out_map, int32_t *out_map_t,
+                   int32_t *out_edge_slot, int32_t *out_window, int32_t *out_atomic,
+                   int32_t *flags, void *stream);
+ATT_API int att_block_fill_result(const int32_t *flags, int with_map_t);
+
 /* ----------------------------------------------------------------------
  * Allocation-free conversion.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory -- hosts that hand out

@@ -142,6 +142,43 @@ def test_async_convert_matches_sync(cuda):
             assert torch.equal(getattr(a, name), getattr(b, name)), (seed, name)
 
 
+def test_async_fill_matches_sync(cuda):
+    """block_convert_finish(check_later=True) (att_block_fill_async: no host
+    synchronisation, checks copied to pinned memory) gives the synchronous
+    format bit for bit, every output included, and its deferred check passes."""
+    import torch
+    from att_gb300 import graphs, ops
+    for seed, (n, L, hubs) in enumerate([(64, 8, 0), (3001, 30, 4), (20000, 12, 10)]):
+        rp, col = graphs.random_csr(n, n, L, seed + 7, hub_rows=hubs, hub_len=min(n, 2000))
+        deg = torch.rand(n, dtype=torch.float32).half()
+        kw = dict(window=8, wide=8, part=32, want_map=True, want_trans=True, want_edge_slot=True)
+        a = ops.block_convert(torch.from_numpy(rp), torch.from_numpy(col), deg, **kw)
+        p = ops.block_convert_async(torch.from_numpy(rp), torch.from_numpy(col), deg, **kw)
+        p.event.synchronize()
+        b = ops.block_convert_finish(p, check_later=True)
+        torch.cuda.synchronize()
+        ops.block_fill_check(b)
+        assert "fill_flags" not in b.extra
+        for name in ("rowptr", "col", "window_of_part", "atomic", "val", "map", "map_t",
+                     "edge_slot"):
+            assert torch.equal(getattr(a, name), getattr(b, name)), (seed, name)
+
+
+def test_async_fill_reports_unsorted_rows_for_mirror_map(cuda):
+    """The deferred check of an asynchronous fill raises what the synchronous
+    fill raises: a mirrored-edge map over unsorted rows."""
+    import torch
+    from att_gb300 import graphs, ops, _lib
+    rowptr, col = graphs.random_csr(64, 64, 8, seed=9, sort_rows=False)
+    p = ops.block_convert_async(torch.from_numpy(rowptr), torch.from_numpy(col), None, window=8,
+                                wide=8, part=32, want_map=True, want_trans=True)
+    p.event.synchronize()
+    f = ops.block_convert_finish(p, check_later=True)
+    torch.cuda.synchronize()
+    with pytest.raises(_lib.AttError):
+        ops.block_fill_check(f)
+
+
 def test_async_convert_rejects_bad_column(cuda):
     import torch
     from att_gb300 import ops, _lib
