@@ -126,8 +126,11 @@ __device__ __forceinline__ int swz_rb(int r) {
 // output); the training path needs it so that dout . out matches the
 // backward's recomputed probabilities.
 // IT: index type of items and element offsets (int32_t when every offset fits)
+// fp32 X' with at most 64 features: registers bounded for 3 CTAs per SM
+// (200 registers would leave room for 2), without spills
 template <typename T, int F, int MODE, bool PSPLIT, typename IT>
-__global__ void __launch_bounds__(kGThreads) k_gat_fused(GatArgs A) {
+__global__ void __launch_bounds__(kGThreads, (sizeof(T) == 4 && F <= 64) ? 3 : 1)
+    k_gat_fused(GatArgs A) {
     using C = GCfg<T, F, MODE>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
