@@ -1491,7 +1491,8 @@ def _serve_form(torch, requests=600, seeds=(4, 5, 6)):
 
 
 def run_forms(torch, stream, steps, warmup, skip=()):
-    """The benchmark spec's chosen forms beside their plain paths, each measured
+    """The chosen forms (bf16 / fp8 SpMM, fused GAT layers, the train step,
+    the serving loop) beside their plain paths, each measured
     on its own workload after the headline one (a few seconds each)."""
     forms = {}
     jobs = [("spmm_products_bf16", lambda: _spmm_form(SpmmProductsBF16, torch, stream, steps, warmup)),
