@@ -1,8 +1,9 @@
 """The reference's own GCN SpMM kernel on the GPU: the "plain FP16 drop-in".
 
-COMPARISON AND TEST INFRASTRUCTURE ONLY (the plain drop-in the bench times beside the product).  ``oracle/build_ref.py`` compiles the
-reference's ``gcn/SpMM/src/spmmKernel.cu`` (unmodified, from the reference
-tree) into the device-only fatbin ``oracle/_ref/ref_spmm.fatbin`` for sm_103a.
+COMPARISON AND TEST INFRASTRUCTURE ONLY (the plain drop-in the bench times
+beside the product).  ``oracle/build_ref.py`` compiles the reference's
+``gcn/SpMM/src/spmmKernel.cu`` (unmodified, from the reference tree) into the
+device-only fatbin ``oracle/_ref/ref_spmm.fatbin`` for sm_103a.
 This module loads that fatbin through the CUDA driver API (ctypes over
 libcuda) and launches its kernels exactly as the reference's binding and
 launcher do:
