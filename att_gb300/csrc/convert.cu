@@ -8,11 +8,11 @@
 // (example.cpp:61-175), this is an integer sort / merge / scan / compaction
 // pipeline:
 //
-//   plan  k_unique_warp    one warp per window of <= kWarpCap edges: bitonic
-//                          sort of (column, edge index) keys in registers,
-//                          de-duplicate, warp-scan compact; each edge's rank
-//                          among its window's distinct columns falls out of
-//                          the sort
+//   plan  k_unique_warp    one warp per window of <= kWarpCap edges (two
+//                          launches by size class): bitonic sort of (column,
+//                          edge index) keys in registers, de-duplicate,
+//                          warp-scan compact; each edge's rank among its
+//                          window's distinct columns falls out of the sort
 //         k_chunk_rows     row holding the first edge of each 2048-edge chunk
 //         k_merge_rank     larger windows, thread per edge: its position in
 //                          the merge of the window's sorted rows (binary
@@ -347,11 +347,28 @@ __global__ void __launch_bounds__(kWarpSortWarps * 32) k_unique_warp(
         window_range(rowptr, w, window, nnz, &b0, &b1, ws.flags);
         const int64_t E = b1 - b0;
         if (E > CAP || E <= LO) continue;  // another kernel's window
-        if constexpr (CAP == kWarpCap) {
-            if (E <= 32) unique_window_regs<KT, 1, IB>(col, b0, (int)E, n_cols, ws, w, lane);
-            else if (E <= 64) unique_window_regs<KT, 2, IB>(col, b0, (int)E, n_cols, ws, w, lane);
-            else if (E <= 128) unique_window_regs<KT, 4, IB>(col, b0, (int)E, n_cols, ws, w, lane);
-            else unique_window_regs<KT, 8, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+        if constexpr (CAP <= kWarpCap) {
+            // only the networks of this launch's size class are compiled in
+            // (one unrolled network per kernel keeps instruction fetch short)
+            if constexpr (LO < 32) {
+                if (E <= 32) {
+                    unique_window_regs<KT, 1, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+                    continue;
+                }
+            }
+            if constexpr (LO < 64 && CAP > 32) {
+                if (E <= 64) {
+                    unique_window_regs<KT, 2, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+                    continue;
+                }
+            }
+            if constexpr (LO < 128 && CAP > 64) {
+                if (E <= 128) {
+                    unique_window_regs<KT, 4, IB>(col, b0, (int)E, n_cols, ws, w, lane);
+                    continue;
+                }
+            }
+            if constexpr (CAP > 128) unique_window_regs<KT, 8, IB>(col, b0, (int)E, n_cols, ws, w, lane);
             continue;
         }
         int n = 32;
@@ -1136,7 +1153,7 @@ int launch_unique_warp(unsigned grid, const int32_t *rowptr, const int32_t *col,
                        int window, int64_t nnz, int64_t n_cols, int unsorted_only, Workspace ws,
                        cudaStream_t st) {
     // register sort up to kWarpCap edges: no shared memory
-    constexpr size_t smem = CAP == kWarpCap ? 0 : (size_t)kWarpSortWarps * CAP * sizeof(KT);
+    constexpr size_t smem = CAP <= kWarpCap ? 0 : (size_t)kWarpSortWarps * CAP * sizeof(KT);
     auto kernel = k_unique_warp<KT, CAP, LO>;
     if (smem > 48 * 1024) {
         static std::once_flag once;
@@ -1210,10 +1227,16 @@ static int plan_enqueue(const int32_t *rowptr, const int32_t *col, int64_t n_row
         // 32-bit keys while (column << index bits) stays below the sentinel
         const bool narrow256 = n_cols <= (1ll << 24) - 1;
         const bool narrow1024 = n_cols <= (1ll << 22) - 1;
-        // windows of <= kWarpCap edges: warp sorts
-        s = narrow256 ? launch_unique_warp<uint32_t, kWarpCap, 0>(g_warp, rowptr, col, nw, window,
-                                                                 nnz, n_cols, 0, ws, st)
-                      : launch_unique_warp<unsigned long long, kWarpCap, 0>(
+        // windows of <= kWarpCap edges: warp sorts in registers, one launch
+        // per size class (up to 128 edges, then 129-256)
+        s = narrow256 ? launch_unique_warp<uint32_t, 128, 0>(g_warp, rowptr, col, nw, window, nnz,
+                                                            n_cols, 0, ws, st)
+                      : launch_unique_warp<unsigned long long, 128, 0>(
+                            g_warp, rowptr, col, nw, window, nnz, n_cols, 0, ws, st);
+        if (s != ATT_OK) return s;
+        s = narrow256 ? launch_unique_warp<uint32_t, kWarpCap, 128>(g_warp, rowptr, col, nw, window,
+                                                                   nnz, n_cols, 0, ws, st)
+                      : launch_unique_warp<unsigned long long, kWarpCap, 128>(
                             g_warp, rowptr, col, nw, window, nnz, n_cols, 0, ws, st);
         if (s != ATT_OK) return s;
         // larger windows: merge ranks, edge-parallel

@@ -42,13 +42,13 @@ from . import _lib, graphs, ops
 from .ops import _p, _stream, require_cuda
 
 GROUP_PARTS = 4  # parts per work group of att_spmm_batched (kGroupParts in spmm.cu)
-# kernels one prepare() launches: conversion 21 for graphs of up to 4M edges
-# (plan: k_unique_warp x2, k_chunk_rows, k_merge_rank, a 3-kernel int32 scan,
+# kernels one prepare() launches: conversion 22 for graphs of up to 4M edges
+# (plan: k_unique_warp x3, k_chunk_rows, k_merge_rank, a 3-kernel int32 scan,
 # k_merge_emit, k_unique_small, k_unique_large, k_window_counts, two 3-kernel
 # int64 scans, k_plan_summary; fill: k_col_chunk_windows, k_fill_cols,
 # k_fill_parts, k_fill_edges) and groups 5 (k_group_flags, a 3-kernel scan,
 # k_group_scatter); a tick launches 3
-PREPARE_LAUNCHES = 26
+PREPARE_LAUNCHES = 27
 TICK_LAUNCHES = 3
 ATT_ERR_FORMAT = 6
 

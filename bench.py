@@ -772,7 +772,7 @@ class ConvertProducts:
         self.bytes_alg = 4 * (rp.shape[0]) + 4 * self.nnz + 2 * rp.shape[0] + self.bytes_out
         self.bytes_compulsory = self.bytes_alg
         self.flops = 0
-        self.launches_per_step = 23  # plan 19 (its int32 scan 5 here) + fill 4
+        self.launches_per_step = 24  # plan 20 (its int32 scan 5 here) + fill 4
         self.config.update({"parts": f.n_parts, "condensed_cols": f.n_condensed,
                             "l2": "inputs and outputs larger than L2 (no flush)"})
 
