@@ -100,6 +100,44 @@ def test_random_graphs_vs_oracle_with_maps(cuda, case):
             assert np.all(mp[es[used]] >= np.nonzero(used)[0])
 
 
+def _windows_of_sizes(sizes, n_cols, seed, sort_rows=True):
+    """CSR whose 8-row windows hold exactly `sizes[i]` edges each, split at
+    random over their rows, columns drawn from a range narrow enough that
+    rows of a window share columns."""
+    rng = np.random.default_rng(seed)
+    lens, cols = [], []
+    for E in sizes:
+        cuts = np.sort(rng.integers(0, E + 1, size=7))
+        per = np.diff(np.concatenate([[0], cuts, [E]]))
+        span = max(8, min(n_cols, 2 * E))
+        lo = int(rng.integers(0, n_cols - span + 1))
+        for L in per:
+            c = rng.integers(lo, lo + span, size=int(L)).astype(np.int32)
+            cols.append(np.sort(c) if sort_rows else c)
+            lens.append(int(L))
+    rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    return rowptr, np.concatenate(cols).astype(np.int32)
+
+
+@pytest.mark.parametrize("sort_rows", [True, False])
+def test_window_sizes_at_every_kernel_boundary(cuda, sort_rows):
+    """Windows of exactly 1, 31-33, 63-65, 127-129, 255-257, 1023-1025 and
+    4095-4097 edges: the edges either side of every size class of the plan
+    (register sorts up to 32, 64, 128 and 256 keys, then the row merge and
+    its sorting / bitmap fallbacks for unsorted rows), with rows sharing
+    columns (duplicates within a window).  Bit-exact with the C oracle."""
+    sizes = [1, 31, 32, 33, 63, 64, 65, 127, 128, 129, 255, 256, 257, 1023, 1024, 1025, 4095,
+             4096, 4097, 0, 7]
+    rowptr, col = _windows_of_sizes(sizes, 20000, seed=31 + sort_rows, sort_rows=sort_rows)
+    d = (1.0 / np.sqrt(np.arange(1, 20001))).astype(np.float32)
+    for (W, w, P, deg, emit) in ((8, 8, 32, d.astype(np.float16), False), (8, 4, 32, d, True)):
+        o = oracle.block_convert(rowptr, col, deg, W, w, P, emit_empty=emit, want_map=True)
+        f = _gpu(rowptr, col, deg, W, w, P, emit, want_map=True, n_cols=deg.shape[0])
+        for name, t in (("rowptr", f.rowptr), ("col", f.col), ("val", f.val),
+                        ("window", f.window_of_part), ("atomic", f.atomic), ("map", f.map)):
+            assert np.array_equal(_bits(t.cpu().numpy()), _bits(o[name])), (sort_rows, W, w, name)
+
+
 def test_unsorted_rows_rejected_for_mirror_map(cuda):
     from att_gb300 import graphs, _lib
     rowptr, col = graphs.random_csr(64, 64, 8, seed=9, sort_rows=False)
